@@ -1,0 +1,367 @@
+"""Benchmark of the DynLP per-batch update path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (default): the reference's default run — n = 50,000 vertices,
+average degree 5, 10 batches, delta 1e-4, maxIter 1e5, tau = mean edge weight,
+seed 42 — generated with the reference generator's exact decisions
+(synthetic; the reference ships no dataset). One step = one replay of the 10
+batches from an empty graph on the plain per-batch path, in the reference's
+semantics. Unit of work: one affected edge, i.e. one (frontier vertex, live
+row entry) visit in propagation, summed over passes and batches — the count is
+fixed by the workload (the oracle produces the same count).
+
+GPU arm: `value` times the batch kernels with the batches already resident in
+HBM (CUDA events on the session stream, L2 flushed by a 512 MiB memset before
+each step); `e2e` replays through the C ABI from host arrays (pinned staging,
+H2D, one kernel per batch, D2H of every batch's statistics and of the final
+labels), wall clock with the stream synchronised on both sides.
+Reference arm (--impl reference): the reference's path is CUDA only, so its
+CPU counterpart is the oracle's restatement of it (oracle/, a port), run with
+all host threads on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "affected-edges/sec and p50/p99 batch-update latency, served vs plain, same GPU"
+UNIT = "affected-edges/s"
+WORKLOADS = {
+    "config2": dict(n=50000, degree=5, batches=10, seed=42),
+    "config1": dict(n=5000, degree=5, batches=10, seed=42),
+    "config3": dict(n=20000000, degree=7, batches=100, seed=42),
+}
+
+
+def workload_desc(name: str) -> str:
+    w = WORKLOADS[name]
+    return (f"{name}: plain per-batch replay, n={w['n']}, avg degree {w['degree']}, {w['batches']} batches "
+            f"(90/1/9 insert/GT/delete), delta 1e-4, maxIter 1e5, tau = mean edge weight, seed {w['seed']}")
+
+
+# ------------------------------------------------------------------ helpers --
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def dist_init(world: int):
+    if world <= 1:
+        return None
+    import torch.distributed as td
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    td.init_process_group("gloo")
+    return td
+
+
+def dist_max(td, x: float) -> float:
+    if td is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(td, x: float) -> float:
+    if td is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.SUM)
+    return float(t.item())
+
+
+def dist_barrier(td):
+    if td is not None:
+        td.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_gbs() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(st: dict, num_edges: int, num_inserted: int) -> int:
+    """Bytes one batch kernel must move at minimum (see the roofline notes):
+    propagation 12 B per affected edge (entry 8 + neighbour label 4) and 20 B
+    per frontier visit (row start/length 8, own old label 4, new label 4,
+    stamp 4); live-row rebuild 16 B per full-graph entry read (read 8, write
+    8); tau filter 28 B per raw edge (src/dst/weight 12, two position lookups
+    8, two position writes 8); label init 16 B per inserted vertex."""
+    return (12 * st["affected_edges"] + 20 * st["frontier_visits"] + 16 * st["dirty_entries"]
+            + 28 * num_edges + 16 * num_inserted)
+
+
+def percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = (len(xs) - 1) * q
+    lo = int(k)
+    hi = min(lo + 1, len(xs) - 1)
+    return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+
+
+# -------------------------------------------------------------- CPU (oracle) --
+
+def cpu_run(problem, threads: int, budget_s: float):
+    """Oracle replay in batch order until the budget is used; returns
+    (affected edges, seconds, batches done)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    orc = pyoracle.OracleRun.from_problem(problem, threads=threads)
+    edges, t0, done = 0, time.perf_counter(), 0
+    for b, bt in enumerate(problem.batches):
+        edges += orc.apply(b, bt)["affected_edges"]
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return edges, time.perf_counter() - t0, done
+
+
+def reference_arm(args, td, rank):
+    import labelpropcuda_gb300 as dlp
+    if rank != 0:
+        return 0
+    w = WORKLOADS[args.workload]
+    p = dlp.Problem(w["n"], w["degree"], w["batches"], w["seed"])
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_run(p, threads, args.ref_budget_s)
+    tot_e, tot_t, per = 0, 0.0, []
+    batches_done = 0
+    for _ in range(args.steps):
+        e, t, done = cpu_run(p, threads, args.ref_budget_s)
+        tot_e += e
+        tot_t += t
+        per.append(t)
+        batches_done = done
+    value = tot_e / tot_t if tot_t > 0 else 0.0
+    sample = (f"oracle port (CPU restatement of the reference's per-batch path), {threads} threads, "
+              f"first {batches_done} of {w['batches']} batches per step (budget {args.ref_budget_s:.0f} s)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (reference generator decisions, seed 42)",
+            "config": {"workload": workload_desc(args.workload), "semantics": "ref"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------- GPU arm -----
+
+def gpu_arm(args, td, rank, world, local_rank):
+    import labelpropcuda_gb300 as dlp
+    from labelpropcuda_gb300 import DeviceArray, DeviceBatch
+    L = dlp._n.lib()
+    dlp._n.check(L.dlp_set_device(local_rank))
+    w = WORKLOADS[args.workload]
+    p = dlp.Problem(w["n"], w["degree"], w["batches"], w["seed"])
+    nb = len(p.batches)
+    sess = dlp.Session.from_problem(p, device=local_rank, narrow_lanes=args.lanes, blocks_per_sm=args.blocks_per_sm)
+    dev_batches = [DeviceBatch(bt) for bt in p.batches]
+    flush = DeviceArray(nbytes=512 << 20)
+
+    def flush_l2():
+        dlp._n.check(L.dlp_memset(flush.ptr, 1, flush.nbytes))
+        dlp._n.check(L.dlp_device_synchronize())
+
+    def device_step():
+        sess.reset()
+        flush_l2()
+        for b in range(nb):
+            sess.apply_device(b, dev_batches[b])
+        sess.synchronize()
+        stats = [sess.stats(b) for b in range(nb)]
+        return sess.elapsed_ms(0, nb - 1), stats
+
+    for _ in range(args.warmup):
+        device_step()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    dist_barrier(td)
+    step_ms, batch_ms, all_stats = [], [], []
+    edges = 0
+    for _ in range(args.steps):
+        ms, stats = device_step()
+        step_ms.append(ms)
+        batch_ms += [s["device_ms"] for s in stats]
+        all_stats.append(stats)
+        edges += sum(s["affected_edges"] for s in stats)
+    dist_barrier(td)
+    clocks = sampler.stop()
+    t_dev = sum(step_ms) / 1e3
+    t_max = dist_max(td, t_dev)
+    edges_all = dist_sum(td, edges)
+    value = edges_all / t_max if t_max > 0 else 0.0
+
+    # end to end: host arrays through the C ABI, statistics read back per batch
+    h2d = sum(bt.nbytes() for bt in p.batches)
+    d2h = nb * 96 + 4 * p.num_nodes
+    for _ in range(max(1, args.warmup // 2)):
+        sess.reset()
+        for b, bt in enumerate(p.batches):
+            sess.apply(b, bt)
+        sess.labels()
+    e2e_s, e2e_edges, e2e_batch_ms = 0.0, 0, []
+    for _ in range(args.steps):
+        sess.reset()
+        flush_l2()
+        t0 = time.perf_counter()
+        for b, bt in enumerate(p.batches):
+            tb = time.perf_counter()
+            st = sess.apply(b, bt)
+            e2e_batch_ms.append(1e3 * (time.perf_counter() - tb))
+            e2e_edges += st["affected_edges"]
+        sess.labels()
+        e2e_s += time.perf_counter() - t0
+    e2e_max = dist_max(td, e2e_s)
+    e2e_value = dist_sum(td, e2e_edges) / e2e_max if e2e_max > 0 else 0.0
+
+    if rank != 0:
+        return 0
+    # roofline of the batch kernel (the only kernel of the timed region)
+    peak, peak_kind = measured_peak_gbs()
+    stats0 = all_stats[-1]
+    bytes_step = sum(algorithmic_bytes(s, bt.edge_src.size, bt.inserted.size) for s, bt in zip(stats0, p.batches))
+    kern_s = sum(s["device_ms"] for s in stats0) / 1e3
+    achieved = bytes_step / kern_s / 1e9 if kern_s > 0 else 0.0
+    traffic = None
+    tf = ROOT / "profiles" / "traffic_batch_kernel_config2.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    # CPU baseline: the oracle, single thread, bounded sample of the same workload
+    cpu_edges, cpu_t, cpu_done = cpu_run(p, 1, args.cpu_budget_s)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (reference generator decisions, seed 42), inputs resident in HBM",
+        "config": {"workload": workload_desc(args.workload), "semantics": "ref", "parallelism": "replicas",
+                   "l2": "flushed before every step (512 MiB memset)", "narrow_lanes": args.lanes or 8,
+                   "blocks_per_sm": args.blocks_per_sm or "occupancy",
+                   "affected_edges_per_step": edges // max(args.steps, 1)},
+        "latency_ms": {"per": "batch", "p50": percentile(batch_ms, 0.5), "p99": percentile(batch_ms, 0.99),
+                       "max": max(batch_ms) if batch_ms else None,
+                       "e2e_p50": percentile(e2e_batch_ms, 0.5), "e2e_p99": percentile(e2e_batch_ms, 0.99)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "timing": "wall clock, stream synchronised on both sides"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "kernel": "dlp::session::batch_kernel", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_step": bytes_step},
+        "cpu_baseline": {"value": cpu_edges / cpu_t if cpu_t > 0 else 0.0, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"oracle port, 1 thread, first {cpu_done} of {nb} batches of the same workload"},
+        "clocks": clocks,
+        "gpu_launches": args.steps * nb,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2")
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--cpu-budget-s", type=float, default=15.0)
+    ap.add_argument("--ref-budget-s", type=float, default=20.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    rank, world, local_rank = dist_env()
+    td = dist_init(world)
+    try:
+        if args.impl == "reference":
+            return reference_arm(args, td, rank)
+        from labelpropcuda_gb300 import build
+        build.build()
+        return gpu_arm(args, td, rank, world, local_rank)
+    finally:
+        if td is not None:
+            td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

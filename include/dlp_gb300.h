@@ -1,0 +1,248 @@
+/*
+ * dlp_gb300.h - C ABI of the GB300-native DynLP per-batch update path.
+ *
+ * Plain pointers and sizes only. Every entry point returns a status code
+ * (DLP_OK on success) instead of exiting; dlp_last_error() holds a message for
+ * the calling thread's last failure. Device pointers are CUDA device
+ * addresses on the current device; `stream` is a cudaStream_t passed as void*
+ * (NULL = the legacy default stream).
+ *
+ * Three groups of entry points:
+ *   1. input generation (host only),
+ *   2. a resident session that keeps one dynamic graph on the GPU and applies
+ *      batches with no host round trip inside a batch,
+ *   3. the reference's five step launchers on caller-owned device arrays in the
+ *      reference's layout (drop-in for src/sparsifySubgraph.cu,
+ *      src/connectedComponents.cu, src/labelInitialization.cu,
+ *      src/iterativePropagation.cu of SMShovan/LabelPropCUDA).
+ * The C++ shims in dynLP.h, sparsifySubgraph.h, connectedComponents.h,
+ * labelInitialization.h and iterativePropagation.h call these.
+ */
+#ifndef DLP_GB300_H
+#define DLP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DLP_ABI_VERSION 1
+
+enum dlp_status {
+  DLP_OK = 0,
+  DLP_ERR_INVALID_ARGUMENT = 1, /* bad size, null pointer, vertex id out of range */
+  DLP_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+  DLP_ERR_OUT_OF_MEMORY = 3,
+  DLP_ERR_TIMEOUT = 4,          /* a device-side wait ran past its limit */
+  DLP_ERR_NO_DEVICE = 5,        /* no usable sm_103 GPU */
+  DLP_ERR_NOT_CONVERGED = 6,    /* connected components exceeded the round cap */
+  DLP_ERR_INTERNAL = 7
+};
+
+enum dlp_semantics {
+  DLP_SEMANTICS_REF = 0,  /* the reference's behaviour (default) */
+  DLP_SEMANTICS_SPEC = 1  /* the documented intent: full affected set, permanent deletions */
+};
+
+int dlp_abi_version(void);
+const char *dlp_status_string(int status);
+/* Message of the calling thread's last failed call ("" if none). */
+const char *dlp_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* 1. Input generation (host). Replaces generateSparseGraph                  */
+/*    (src/generateSparseGraph.cu:118) and generateBatches                   */
+/*    (src/generateBatches.cu:44) with the same seeded output.               */
+/* ------------------------------------------------------------------------ */
+
+typedef struct dlp_problem dlp_problem;
+
+/* A batch as plain arrays (host or device pointers, depending on the call). */
+typedef struct dlp_batch_view {
+  const int *inserted;       /* vertices that arrive in this batch */
+  int num_inserted;
+  const int *gt_ids;         /* subset of inserted with ground-truth labels */
+  const float *gt_labels;    /* 0.0 / 1.0 */
+  int num_gt;
+  const int *deleted;        /* vertices removed in this batch */
+  int num_deleted;
+  const int *edge_src;       /* edges that become live in this batch (src < dst) */
+  const int *edge_dst;
+  const float *edge_weight;
+  int num_edges;
+} dlp_batch_view;
+
+int dlp_problem_generate(int num_nodes, int avg_degree, int num_batches, unsigned seed,
+                         float gt_fraction, float deleted_fraction, dlp_problem **out);
+void dlp_problem_free(dlp_problem *p);
+int dlp_problem_num_nodes(const dlp_problem *p);
+int64_t dlp_problem_num_edges(const dlp_problem *p);
+int dlp_problem_num_batches(const dlp_problem *p);
+const int *dlp_problem_row_ptr(const dlp_problem *p);
+const int *dlp_problem_col_ind(const dlp_problem *p);
+const float *dlp_problem_values(const dlp_problem *p);
+const float *dlp_problem_true_labels(const dlp_problem *p);
+/* Host views into the problem's storage (valid until dlp_problem_free). */
+int dlp_problem_batch(const dlp_problem *p, int batch, dlp_batch_view *out);
+/* <prefix>RowPtr.txt, ColInd.txt, Values.txt, TrueLabels.txt in the reference's
+ * text format (src/generateSparseGraph.cu:224-271). */
+int dlp_problem_write_csr(const dlp_problem *p, const char *prefix);
+/* Mean weight of the non-deleted edges of a CSR (auto tau, src/dynLP.cu:90-102). */
+float dlp_mean_edge_weight(int64_t num_edges, const int *col_ind, const float *values);
+
+/* ------------------------------------------------------------------------ */
+/* 2. Resident session: one dynamic graph on the GPU                          */
+/*    (the per-batch loop of runDynLP, src/dynLP.cu:284-558).                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct dlp_config {
+  float tau;             /* sparsification threshold; < 0: mean full-graph edge weight */
+  float delta;           /* convergence threshold (> 0) */
+  int max_iterations;    /* propagation pass cap */
+  int semantics;         /* enum dlp_semantics */
+  int device;            /* CUDA device ordinal */
+  int record;            /* nonzero: keep per-batch artefacts for dlp_session_artefact */
+  int narrow_lanes;      /* lanes per short row in propagation: 4, 8, 16 or 32; 0 = tuned */
+  int blocks_per_sm;     /* persistent grid occupancy; 0 = from the occupancy query */
+  double wait_timeout_s; /* limit for any device-side wait; <= 0: 2 s */
+} dlp_config;
+
+void dlp_config_default(dlp_config *cfg);
+
+/* Per-batch results. */
+typedef struct dlp_batch_stats {
+  int batch;
+  int iterations;          /* propagation passes (iterationsUsed) */
+  int num_components;      /* connected components among inserted vertices */
+  int num_sub_edges;       /* 2 x new-new edges with w > tau (numSubEdges) */
+  int hook_edges;          /* edges hooked by the components step */
+  int hook_rounds;         /* hook passes until no change */
+  int seed_frontier;       /* |F_0| */
+  int seed_marks;          /* vertices marked affected before filtering */
+  int64_t affected_edges;  /* sum over passes of the frontier's row lengths */
+  int64_t frontier_visits; /* sum over passes of the frontier size */
+  int64_t correct;         /* active non-GT vertices on the right side of 0.5 */
+  int64_t total;           /* active non-GT vertices */
+  float accuracy;          /* correct / total (1 when total == 0) */
+  int status;              /* DLP_OK or the device-reported error */
+  int init_branch;         /* 0 none, 1 component init, 2 no-edge init */
+  int hook_truncated;      /* ref: num_sub_edges exceeded the batch's edge count */
+  float device_ms;         /* device time of the batch kernel */
+  int dirty_rows;          /* live rows rebuilt (changed vertices and their neighbours) */
+  int64_t dirty_entries;   /* full-graph entries read by that rebuild */
+} dlp_batch_stats;
+
+typedef struct dlp_session dlp_session;
+
+/* Uploads the full graph (host CSR, int32 rows sorted by column) and creates the
+ * resident state. true_labels (may be NULL) feeds the accuracy counters.
+ * vertex_batch_map (may be NULL) gives the batch in which each vertex arrives
+ * (-1: never); with it a vertex is live in batch b only if it arrived by b, as
+ * the reference's host rebuild requires (src/dynLP.cu:143-145). */
+int dlp_session_create(const dlp_config *cfg, int num_nodes, int64_t num_edges,
+                       const int *row_ptr, const int *col_ind, const float *values,
+                       const float *true_labels, const int *vertex_batch_map,
+                       dlp_session **out);
+int dlp_session_destroy(dlp_session *s);
+/* Back to the state before the first batch (graph stays resident). */
+int dlp_session_reset(dlp_session *s);
+float dlp_session_tau(const dlp_session *s);
+/* Applies batch `batch_index` from host arrays: copies them to the device,
+ * runs the whole batch as one persistent kernel, and (if stats != NULL) waits
+ * and returns the batch's statistics. */
+int dlp_session_apply_batch(dlp_session *s, int batch_index, const dlp_batch_view *host_batch,
+                            dlp_batch_stats *stats);
+/* Same with device-resident batch arrays; never waits. */
+int dlp_session_apply_batch_device(dlp_session *s, int batch_index,
+                                   const dlp_batch_view *device_batch);
+/* Waits for queued batches; then dlp_session_stats returns any batch's numbers. */
+int dlp_session_synchronize(dlp_session *s);
+int dlp_session_stats(dlp_session *s, int batch_index, dlp_batch_stats *out);
+int dlp_session_read_labels(dlp_session *s, float *host_labels);
+void *dlp_session_stream(dlp_session *s);
+/* Device time from the start of the latest application of batch `first` to the
+ * end of the latest application of batch `last` (CUDA events on the session
+ * stream); waits for the stream. */
+int dlp_session_elapsed_ms(dlp_session *s, int first, int last, float *ms);
+
+/* Artefacts of the last applied batch when cfg.record != 0 (4-byte elements;
+ * *count receives the element count; host_out may be NULL to query it). */
+enum dlp_artefact {
+  DLP_ART_SEED_MARKS = 0,   /* int32 ascending */
+  DLP_ART_FRONTIER0 = 1,    /* int32 ascending */
+  DLP_ART_SUB_EDGES = 2,    /* int32 pairs (u,v),(v,u) in raw edge order */
+  DLP_ART_COMP_ROOT = 3,    /* int32 per inserted vertex: min vertex id of its component, -1 */
+  DLP_ART_INIT_LABELS = 5,  /* fp32 per inserted vertex */
+  DLP_ART_FRONTIER_SIZES = 6,
+  DLP_ART_ROW_LENGTHS = 7,  /* int32 per vertex: live row length (before soft delete) */
+  DLP_ART_LABELS = 10
+};
+int dlp_session_artefact(dlp_session *s, int which, void *host_out, int64_t capacity,
+                         int64_t *count);
+
+/* ------------------------------------------------------------------------ */
+/* 3. Step launchers on caller-owned device arrays, reference layout.        */
+/*    Same argument meaning as the reference; they synchronise the stream    */
+/*    only where a scalar result is returned through a pointer.             */
+/* ------------------------------------------------------------------------ */
+
+/* launchMarkDeletions (src/sparsifySubgraph.cu:185-203). */
+int dlp_mark_deletions(int *d_row_ptr, int *d_col_ind, int *d_vertex_status, int *d_is_affected,
+                       const int *d_deleted_nodes, int num_deleted, int num_nodes, void *stream);
+
+/* launchBuildSparsifiedSubgraph (src/sparsifySubgraph.cu:205-287). The kept
+ * edges are written to d_sub_col_ind / d_sub_values (destinations and weights,
+ * both directions, raw edge order; each at least max(2*num_new_edges,1) long). */
+int dlp_build_sparsified_subgraph(int *d_row_ptr, int *d_col_ind, float *d_values,
+                                  int *d_is_affected, const int *d_vertex_status,
+                                  const int *d_new_edge_src, const int *d_new_edge_dst,
+                                  const float *d_new_edge_weight, int num_new_edges,
+                                  const int *d_inserted_nodes, int num_inserted,
+                                  const int *d_is_new_vertex, float tau, int *d_sub_row_ptr,
+                                  int *d_sub_col_ind, float *d_sub_values, int *num_sub_nodes,
+                                  int *num_sub_edges, void *stream);
+
+/* launchConnectedComponents (src/connectedComponents.cu:162-290). */
+int dlp_connected_components(const int *d_edge_src, const int *d_edge_dst, int num_edges,
+                             const int *d_inserted_nodes, int num_inserted, int *d_component_id,
+                             int *num_components, int num_nodes, void *stream);
+
+/* launchLabelInitialization (src/labelInitialization.cu:148-187). */
+int dlp_label_initialization(const int *d_row_ptr, const int *d_col_ind, const float *d_values,
+                             float *d_labels, const int *d_vertex_status,
+                             const int *d_component_id, int num_components,
+                             const int *d_inserted_nodes, int num_inserted, const int *d_gt_class,
+                             int num_nodes, void *stream);
+
+/* launchIterativePropagation (src/iterativePropagation.cu:241-346). */
+int dlp_iterative_propagation(const int *d_row_ptr, const int *d_col_ind, const float *d_values,
+                              float *d_labels, float *d_labels_buffer, const int *d_vertex_status,
+                              const int *d_gt_class, int *d_is_affected, int num_nodes,
+                              float delta, int max_iterations, int *iterations_used,
+                              void *stream);
+
+/* launchIrLP (src/validation.cu:145-208): full recompute of every active
+ * non-ground-truth vertex per iteration until no label moves by more than
+ * delta, as one cooperative launch. Result in d_labels. */
+int dlp_irlp(const int *d_row_ptr, const int *d_col_ind, const float *d_values, float *d_labels,
+             const int *d_vertex_status, const int *d_gt_class, int num_nodes, float delta,
+             int max_iterations, int *iterations_used, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Device helpers for bindings that have no CUDA runtime of their own.       */
+/* ------------------------------------------------------------------------ */
+int dlp_device_count(int *count);
+int dlp_set_device(int device);
+int dlp_malloc(void **ptr, size_t bytes);
+int dlp_free(void *ptr);
+int dlp_memcpy_htod(void *dst, const void *src, size_t bytes);
+int dlp_memcpy_dtoh(void *dst, const void *src, size_t bytes);
+int dlp_memset(void *ptr, int value, size_t bytes);
+int dlp_device_synchronize(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DLP_GB300_H */

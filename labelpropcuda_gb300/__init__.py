@@ -1,0 +1,267 @@
+"""GB300-native DynLP per-batch update path (Python binding of the C ABI).
+
+The compute lives in libdynlp_gb300.so (hand-written sm_103a CUDA); this
+package wraps its C ABI for tests, benchmarks and Python callers:
+
+    Problem   seeded synthetic graph + batches (the reference generator's output)
+    Session   one dynamic graph resident on the GPU; apply() runs a whole batch
+    DeviceArray  a device buffer for the step launchers and device-resident inputs
+    launchers    the reference's five step launchers on device arrays
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as _n
+from ._native import DlpError, SEMANTICS_REF, SEMANTICS_SPEC  # noqa: F401
+
+__all__ = ["Problem", "Session", "DeviceArray", "DlpError", "SEMANTICS_REF", "SEMANTICS_SPEC",
+           "device_count", "batch_map"]
+
+
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None or a.size == 0 else a.ctypes.data
+
+
+def device_count() -> int:
+    c = ctypes.c_int(0)
+    _n.check(_n.lib().dlp_device_count(ctypes.byref(c)))
+    return c.value
+
+
+@dataclass
+class Batch:
+    inserted: np.ndarray
+    gt_ids: np.ndarray
+    gt_labels: np.ndarray
+    deleted: np.ndarray
+    edge_src: np.ndarray
+    edge_dst: np.ndarray
+    edge_weight: np.ndarray
+
+    @staticmethod
+    def make(inserted=(), gt_ids=(), gt_labels=(), deleted=(), edge_src=(), edge_dst=(), edge_weight=()):
+        i32 = lambda x: np.ascontiguousarray(np.asarray(x, dtype=np.int32).reshape(-1))
+        f32 = lambda x: np.ascontiguousarray(np.asarray(x, dtype=np.float32).reshape(-1))
+        return Batch(i32(inserted), i32(gt_ids), f32(gt_labels), i32(deleted), i32(edge_src), i32(edge_dst),
+                     f32(edge_weight))
+
+    def view(self) -> _n.BatchView:
+        v = _n.BatchView()
+        v.inserted, v.num_inserted = _ptr(self.inserted), self.inserted.size
+        v.gt_ids, v.gt_labels, v.num_gt = _ptr(self.gt_ids), _ptr(self.gt_labels), self.gt_ids.size
+        v.deleted, v.num_deleted = _ptr(self.deleted), self.deleted.size
+        v.edge_src, v.edge_dst, v.edge_weight = _ptr(self.edge_src), _ptr(self.edge_dst), _ptr(self.edge_weight)
+        v.num_edges = self.edge_src.size
+        return v
+
+    def nbytes(self) -> int:
+        return sum(a.nbytes for a in (self.inserted, self.gt_ids, self.gt_labels, self.deleted, self.edge_src,
+                                      self.edge_dst, self.edge_weight))
+
+
+class Problem:
+    """Seeded synthetic input: full CSR graph, true labels and the batch list,
+    identical to the reference generator's output for the same arguments."""
+
+    def __init__(self, num_nodes: int, avg_degree: int, num_batches: int, seed: int = 42,
+                 gt_fraction: float = 0.01, deleted_fraction: float = 0.09):
+        L = _n.lib()
+        h = ctypes.c_void_p()
+        _n.check(L.dlp_problem_generate(num_nodes, avg_degree, num_batches, seed, gt_fraction, deleted_fraction,
+                                        ctypes.byref(h)))
+        try:
+            self.num_nodes = L.dlp_problem_num_nodes(h)
+            m = L.dlp_problem_num_edges(h)
+            n = self.num_nodes
+            cp = lambda p, cnt, t: np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(t)), (cnt,)).copy() \
+                if cnt else np.zeros(0, dtype=np.dtype(t))
+            self.row_ptr = cp(L.dlp_problem_row_ptr(h), n + 1, ctypes.c_int32)
+            self.col_ind = cp(L.dlp_problem_col_ind(h), m, ctypes.c_int32)
+            self.values = cp(L.dlp_problem_values(h), m, ctypes.c_float)
+            self.true_labels = cp(L.dlp_problem_true_labels(h), n, ctypes.c_float)
+            self.batches: list[Batch] = []
+            for b in range(L.dlp_problem_num_batches(h)):
+                v = _n.BatchView()
+                _n.check(L.dlp_problem_batch(h, b, ctypes.byref(v)))
+                self.batches.append(Batch(
+                    cp(v.inserted, v.num_inserted, ctypes.c_int32), cp(v.gt_ids, v.num_gt, ctypes.c_int32),
+                    cp(v.gt_labels, v.num_gt, ctypes.c_float), cp(v.deleted, v.num_deleted, ctypes.c_int32),
+                    cp(v.edge_src, v.num_edges, ctypes.c_int32), cp(v.edge_dst, v.num_edges, ctypes.c_int32),
+                    cp(v.edge_weight, v.num_edges, ctypes.c_float)))
+        finally:
+            L.dlp_problem_free(h)
+
+    @property
+    def num_edges(self) -> int:
+        return int(self.col_ind.size)
+
+    def batch_map(self) -> np.ndarray:
+        return batch_map(self.num_nodes, self.batches)
+
+
+def batch_map(num_nodes: int, batches: list[Batch]) -> np.ndarray:
+    """Batch of (last) arrival per vertex, -1 if never (src/dynLP.cu:193-198)."""
+    m = np.full(num_nodes, -1, dtype=np.int32)
+    for b, bt in enumerate(batches):
+        m[bt.inserted] = b
+    return m
+
+
+class Session:
+    """One dynamic graph resident on the GPU (dlp_session_*)."""
+
+    def __init__(self, num_nodes: int, row_ptr, col_ind, values, true_labels=None, vertex_batch_map=None, *,
+                 tau: float = -1.0, delta: float = 1e-4, max_iterations: int = 100000,
+                 semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False, narrow_lanes: int = 0,
+                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0):
+        L = _n.lib()
+        cfg = _n.Config()
+        L.dlp_config_default(ctypes.byref(cfg))
+        cfg.tau, cfg.delta, cfg.max_iterations = tau, delta, max_iterations
+        cfg.semantics, cfg.device, cfg.record = semantics, device, int(bool(record))
+        cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
+        self._keep = [np.ascontiguousarray(row_ptr, dtype=np.int32), np.ascontiguousarray(col_ind, dtype=np.int32),
+                      np.ascontiguousarray(values, dtype=np.float32)]
+        tl = None if true_labels is None else np.ascontiguousarray(true_labels, dtype=np.float32)
+        bm = None if vertex_batch_map is None else np.ascontiguousarray(vertex_batch_map, dtype=np.int32)
+        self.num_nodes = num_nodes
+        self._h = ctypes.c_void_p()
+        _n.check(L.dlp_session_create(ctypes.byref(cfg), num_nodes, self._keep[1].size, self._keep[0].ctypes.data,
+                                      _ptr(self._keep[1]), _ptr(self._keep[2]), _ptr(tl), _ptr(bm),
+                                      ctypes.byref(self._h)))
+        self._keep = None
+
+    @classmethod
+    def from_problem(cls, p: Problem, **kw) -> "Session":
+        return cls(p.num_nodes, p.row_ptr, p.col_ind, p.values, p.true_labels, p.batch_map(), **kw)
+
+    def close(self) -> None:
+        if self._h:
+            _n.lib().dlp_session_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def tau(self) -> float:
+        return float(_n.lib().dlp_session_tau(self._h))
+
+    def reset(self) -> None:
+        _n.check(_n.lib().dlp_session_reset(self._h))
+
+    def apply(self, batch_index: int, batch: Batch, wait: bool = True) -> dict | None:
+        v = batch.view()
+        if wait:
+            st = _n.BatchStats()
+            _n.check(_n.lib().dlp_session_apply_batch(self._h, batch_index, ctypes.byref(v), ctypes.byref(st)))
+            return st.as_dict()
+        _n.check(_n.lib().dlp_session_apply_batch(self._h, batch_index, ctypes.byref(v), None))
+        return None
+
+    def apply_device(self, batch_index: int, dbatch: "DeviceBatch") -> None:
+        v = dbatch.view()
+        _n.check(_n.lib().dlp_session_apply_batch_device(self._h, batch_index, ctypes.byref(v)))
+
+    def synchronize(self) -> None:
+        _n.check(_n.lib().dlp_session_synchronize(self._h))
+
+    def stats(self, batch_index: int) -> dict:
+        st = _n.BatchStats()
+        _n.check(_n.lib().dlp_session_stats(self._h, batch_index, ctypes.byref(st)))
+        return st.as_dict()
+
+    def elapsed_ms(self, first: int, last: int) -> float:
+        ms = ctypes.c_float(0.0)
+        _n.check(_n.lib().dlp_session_elapsed_ms(self._h, first, last, ctypes.byref(ms)))
+        return float(ms.value)
+
+    def labels(self) -> np.ndarray:
+        out = np.empty(self.num_nodes, dtype=np.float32)
+        _n.check(_n.lib().dlp_session_read_labels(self._h, out.ctypes.data))
+        return out
+
+    def artefact(self, which: int) -> np.ndarray:
+        cnt = ctypes.c_int64(0)
+        _n.check(_n.lib().dlp_session_artefact(self._h, which, None, 0, ctypes.byref(cnt)))
+        dt = np.float32 if which in (_n.ART_INIT_LABELS, _n.ART_LABELS) else np.int32
+        out = np.empty(cnt.value, dtype=dt)
+        if cnt.value:
+            _n.check(_n.lib().dlp_session_artefact(self._h, which, out.ctypes.data, cnt.value, ctypes.byref(cnt)))
+        return out
+
+
+class DeviceArray:
+    """A device buffer owned by Python (dlp_malloc / dlp_free)."""
+
+    def __init__(self, host: np.ndarray | None = None, *, nbytes: int | None = None, dtype=None, count=None):
+        L = _n.lib()
+        if host is not None:
+            host = np.ascontiguousarray(host)
+            self.dtype, self.count, nbytes = host.dtype, host.size, host.nbytes
+        else:
+            self.dtype = np.dtype(dtype) if dtype is not None else np.dtype(np.uint8)
+            self.count = count if count is not None else nbytes // self.dtype.itemsize
+            nbytes = self.count * self.dtype.itemsize
+        self.nbytes = nbytes
+        self.ptr = ctypes.c_void_p()
+        _n.check(L.dlp_malloc(ctypes.byref(self.ptr), max(nbytes, 16)))
+        if host is not None and nbytes:
+            _n.check(L.dlp_memcpy_htod(self.ptr, host.ctypes.data, nbytes))
+
+    @property
+    def addr(self) -> int:
+        return self.ptr.value or 0
+
+    def get(self) -> np.ndarray:
+        out = np.empty(self.count, dtype=self.dtype)
+        if self.nbytes:
+            _n.check(_n.lib().dlp_memcpy_dtoh(out.ctypes.data, self.ptr, self.nbytes))
+        return out
+
+    def set(self, host: np.ndarray) -> None:
+        host = np.ascontiguousarray(host, dtype=self.dtype)
+        assert host.nbytes <= self.nbytes
+        _n.check(_n.lib().dlp_memcpy_htod(self.ptr, host.ctypes.data, host.nbytes))
+
+    def free(self) -> None:
+        if self.ptr:
+            _n.lib().dlp_free(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class DeviceBatch:
+    """A batch uploaded once to device memory (for device-resident replays)."""
+
+    def __init__(self, batch: Batch):
+        self.parts = [DeviceArray(a) for a in (batch.inserted, batch.gt_ids, batch.gt_labels, batch.deleted,
+                                               batch.edge_src, batch.edge_dst, batch.edge_weight)]
+        self.sizes = (batch.inserted.size, batch.gt_ids.size, batch.deleted.size, batch.edge_src.size)
+
+    def view(self) -> _n.BatchView:
+        p = [a.addr for a in self.parts]
+        v = _n.BatchView()
+        v.inserted, v.num_inserted = p[0], self.sizes[0]
+        v.gt_ids, v.gt_labels, v.num_gt = p[1], p[2], self.sizes[1]
+        v.deleted, v.num_deleted = p[3], self.sizes[2]
+        v.edge_src, v.edge_dst, v.edge_weight, v.num_edges = p[4], p[5], p[6], self.sizes[3]
+        return v
