@@ -117,13 +117,14 @@ class Session:
     def __init__(self, num_nodes: int, row_ptr, col_ind, values, true_labels=None, vertex_batch_map=None, *,
                  tau: float = -1.0, delta: float = 1e-4, max_iterations: int = 100000,
                  semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False, narrow_lanes: int = 0,
-                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0):
+                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: bool = True):
         L = _n.lib()
         cfg = _n.Config()
         L.dlp_config_default(ctypes.byref(cfg))
         cfg.tau, cfg.delta, cfg.max_iterations = tau, delta, max_iterations
         cfg.semantics, cfg.device, cfg.record = semantics, device, int(bool(record))
         cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
+        cfg.small_frontier_solo = int(bool(small_frontier_solo))
         self._keep = [np.ascontiguousarray(row_ptr, dtype=np.int32), np.ascontiguousarray(col_ind, dtype=np.int32),
                       np.ascontiguousarray(values, dtype=np.float32)]
         tl = None if true_labels is None else np.ascontiguousarray(true_labels, dtype=np.float32)
@@ -226,15 +227,18 @@ class DeviceArray:
     def addr(self) -> int:
         return self.ptr.value or 0
 
-    def get(self) -> np.ndarray:
-        out = np.empty(self.count, dtype=self.dtype)
+    def get(self, dtype=None) -> np.ndarray:
+        dt = np.dtype(dtype) if dtype is not None else self.dtype
+        out = np.empty(self.nbytes // dt.itemsize, dtype=dt)
         if self.nbytes:
-            _n.check(_n.lib().dlp_memcpy_dtoh(out.ctypes.data, self.ptr, self.nbytes))
+            _n.check(_n.lib().dlp_memcpy_dtoh(out.ctypes.data, self.ptr, out.nbytes))
         return out
 
     def set(self, host: np.ndarray) -> None:
-        host = np.ascontiguousarray(host, dtype=self.dtype)
-        assert host.nbytes <= self.nbytes
+        """Copies the host array's bytes (no dtype conversion)."""
+        host = np.ascontiguousarray(host)
+        if host.nbytes > self.nbytes:
+            raise ValueError("host array larger than the device buffer")
         _n.check(_n.lib().dlp_memcpy_htod(self.ptr, host.ctypes.data, host.nbytes))
 
     def free(self) -> None:

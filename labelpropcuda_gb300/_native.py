@@ -33,7 +33,7 @@ class Config(ctypes.Structure):
         ("tau", ctypes.c_float), ("delta", ctypes.c_float), ("max_iterations", ctypes.c_int),
         ("semantics", ctypes.c_int), ("device", ctypes.c_int), ("record", ctypes.c_int),
         ("narrow_lanes", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-        ("wait_timeout_s", ctypes.c_double),
+        ("wait_timeout_s", ctypes.c_double), ("small_frontier_solo", ctypes.c_int),
     ]
 
 

@@ -282,6 +282,7 @@ int launch_batch(dlp_session *s, int batch_index, const dlp_batch_view *dv) {
   a.max_iter = s->cfg.max_iterations;
   a.spec = s->cfg.semantics == DLP_SEMANTICS_SPEC;
   a.record = s->cfg.record != 0;
+  a.solo = s->cfg.small_frontier_solo != 0;
   const double to = s->cfg.wait_timeout_s > 0 ? s->cfg.wait_timeout_s : 2.0;
   a.timeout_ns = static_cast<unsigned long long>(to * 1e9);
 
@@ -324,6 +325,7 @@ void dlp_config_default(dlp_config *cfg) {
   cfg->narrow_lanes = 0;
   cfg->blocks_per_sm = 0;
   cfg->wait_timeout_s = 2.0;
+  cfg->small_frontier_solo = 1;
 }
 
 int dlp_session_create(const dlp_config *cfg_in, int n, int64_t m, const int *row_ptr,

@@ -504,23 +504,301 @@ __device__ void phase_f(const View &w, const Ctx &c, bool comp_path) {
 
 // ---------------------------------------------------------------- phase G ---
 // Frontier propagation until the frontier is empty (src/iterativePropagation.cu:274-327).
+
+// One row of at most 32 live entries by a group of G lanes: new label into
+// dst, then mark(cand, v) for each entry and for u itself (called by every
+// lane, the same number of times). Returns whether u moved by more than delta.
+template <int G, class Mark>
+__device__ __forceinline__ void narrow_row(const DevState &s, const float *src, float *dst, float delta, int u,
+                                           bool valid, int gl, unsigned long long &edges,
+                                           unsigned long long &visits, Mark mark) {
+  constexpr int R = 32 / G;
+  int rs = 0, len = 0;
+  if (valid) {
+    rs = s.full_row[u];
+    len = s.act_len[u];
+  }
+  float sw[R], sl[R];
+  int vv[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int e = gl + G * r;
+    sw[r] = 0.0f;
+    sl[r] = 0.0f;
+    vv[r] = -1;
+    if (e < len) {
+      const int2 ent = s.act_adj[rs + e];
+      vv[r] = ent.x;
+      if (ent.x >= 0) {
+        const float wt = __int_as_float(ent.y);
+        sw[r] = wt;                                // 0 + w
+        sl[r] = __fmaf_rn(wt, src[ent.x], 0.0f);   // fma(w, F_v, 0)
+      }
+    }
+  }
+#pragma unroll
+  for (int half = R / 2; half >= 1; half >>= 1)
+#pragma unroll
+    for (int r = 0; r < half; ++r) {
+      sw[r] = sw[r] + sw[r + half];
+      sl[r] = sl[r] + sl[r + half];
+    }
+  float tw = sw[0], tl = sl[0];
+#pragma unroll
+  for (int o = G / 2; o >= 1; o >>= 1) {
+    tw = tw + __shfl_down_sync(0xffffffffu, tw, o, G);
+    tl = tl + __shfl_down_sync(0xffffffffu, tl, o, G);
+  }
+  int changed = 0;
+  if (valid && gl == 0) {
+    const float old = src[u];
+    const float nl = updated_label(tw, tl, old);
+    dst[u] = nl;
+    changed = fabsf(nl - old) > delta;
+    edges += static_cast<unsigned long long>(len);
+    visits += 1ull;
+  }
+  changed = __shfl_sync(0xffffffffu, changed, 0, G);
+  // changed vertex: non-deleted, non-GT neighbours and itself
+  // (src/iterativePropagation.cu:200-216)
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int v = vv[r];
+    mark(changed && v >= 0 && s.gt[v] < 0, v);
+  }
+  mark(changed && gl == 0, u);
+}
+
+// One row of any length by a whole warp: 256 slots held as lane + 32*j.
+template <class Mark>
+__device__ __forceinline__ void wide_row(const DevState &s, const float *src, float *dst, float delta, int u,
+                                         int lane, unsigned long long &edges, unsigned long long &visits,
+                                         Mark mark) {
+  const int rs = s.full_row[u];
+  const int len = s.act_len[u];
+  float sw[8], sl[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) sw[j] = sl[j] = 0.0f;
+  for (int p = 0; p < len; p += 256) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int e = p + j * 32 + lane;
+      if (e < len) {
+        const int2 ent = s.act_adj[rs + e];
+        if (ent.x >= 0) {
+          const float wt = __int_as_float(ent.y);
+          sw[j] = sw[j] + wt;
+          sl[j] = __fmaf_rn(wt, src[ent.x], sl[j]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int half = 4; half >= 1; half >>= 1)
+#pragma unroll
+    for (int j = 0; j < half; ++j) {
+      sw[j] = sw[j] + sw[j + half];
+      sl[j] = sl[j] + sl[j + half];
+    }
+  float tw = sw[0], tl = sl[0];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    tw = tw + __shfl_down_sync(0xffffffffu, tw, o);
+    tl = tl + __shfl_down_sync(0xffffffffu, tl, o);
+  }
+  int changed = 0;
+  if (lane == 0) {
+    const float old = src[u];
+    const float nl = updated_label(tw, tl, old);
+    dst[u] = nl;
+    changed = fabsf(nl - old) > delta;
+    edges += static_cast<unsigned long long>(len);
+    visits += 1ull;
+  }
+  changed = __shfl_sync(0xffffffffu, changed, 0);
+  if (changed) {
+    for (int e0 = 0; e0 < len; e0 += 32) {
+      const int e = e0 + lane;
+      const int v = e < len ? s.act_adj[rs + e].x : -1;
+      mark(v >= 0 && s.gt[v] < 0, v);
+    }
+    mark(lane == 0, u);
+  }
+}
+
+// Solo mode: small frontiers are run by block 0 alone, pass after pass, with
+// __syncthreads() between passes and the frontier and its dedup set in shared
+// memory, while the other blocks wait at the next grid barrier. The passes and
+// their arithmetic are exactly those of the grid path; only the
+// synchronisation changes. Solo mode ends at the first pass whose frontier is
+// too large for the shared buffers, when the frontier empties, at max_iter,
+// or after kSoloBudgetNs, and hands the frontier back through the global set.
+constexpr int kSoloEntry = 128;       // enter when the frontier is at most this
+constexpr int kSoloLive = 512;        // leave when it grows above this
+constexpr int kSoloCap = 1024;        // shared frontier capacity (next pass bound)
+constexpr int kSoloHash = 2048;       // per-pass dedup table
+constexpr int kSoloSeen = 2048;       // vertices that entered a frontier in solo mode
+constexpr unsigned long long kSoloBudgetNs = 100000000ull;
+
+struct SoloShared {
+  int list[2][kSoloCap];
+  int hash[kSoloHash];
+  int seen[kSoloSeen];
+  int cnt[2][2];
+  int seen_n;
+  int stop;
+  int bound;
+};
+
+__device__ __forceinline__ unsigned mix32(unsigned x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// Inserts v into an open-addressing table of `size` slots (-1 = empty);
+// returns true when v was not present. The caller bounds the load.
+__device__ __forceinline__ bool shared_insert(int *table, int size, int v) {
+  unsigned h = mix32(static_cast<unsigned>(v)) & static_cast<unsigned>(size - 1);
+  for (int probe = 0; probe < size; ++probe) {
+    const int prev = atomicCAS(&table[h], -1, v);
+    if (prev == -1) return true;
+    if (prev == v) return false;
+    h = (h + 1) & static_cast<unsigned>(size - 1);
+  }
+  return false;
+}
+
 template <int G>
-__device__ bool phase_g(const View &w, const Ctx &c, int &iterations, unsigned long long &edges,
-                        unsigned long long &visits) {
+__device__ int solo_passes(const View &w, int k0, SoloShared &sh, unsigned long long &edges,
+                           unsigned long long &visits) {
   const DevState &s = w.s;
   const BatchArgs &a = w.a;
   const int n = s.n;
-  constexpr int R = 32 / G;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int GPW = 32 / G;
+  const int grp = lane / G, gl = lane & (G - 1);
+  const int cb = s.ctl->cur_buf;
+  // take over F_k0 from the global set
+  {
+    const int set = k0 % 3;
+    const int nn = ld_relaxed_i32(&s.bc->front_count[set][0]);
+    const int nw = ld_relaxed_i32(&s.bc->front_count[set][1]);
+    const int *gl_list = s.flist + static_cast<size_t>(set) * n;
+    for (int i = tid; i < nn; i += blockDim.x) sh.list[0][i] = gl_list[i];
+    for (int i = tid; i < nw; i += blockDim.x) sh.list[0][kSoloCap - 1 - i] = gl_list[n - 1 - i];
+    for (int i = tid; i < kSoloSeen; i += blockDim.x) sh.seen[i] = -1;
+    if (tid == 0) {
+      sh.cnt[0][0] = nn;
+      sh.cnt[0][1] = nw;
+      sh.seen_n = 0;
+    }
+  }
+  __syncthreads();
+  const uint64_t t0 = global_timer_ns();
+  int k = k0;
+  int p = 0;
+  for (;; ++k, p ^= 1) {
+    const int nn = sh.cnt[p][0], nw = sh.cnt[p][1];
+    // next-frontier bound: every live entry of every frontier row, plus the rows
+    if (tid == 0) sh.bound = nn + nw;
+    __syncthreads();
+    int part = 0;
+    for (int i = tid; i < nn; i += blockDim.x) part += s.act_len[sh.list[p][i]];
+    for (int i = tid; i < nw; i += blockDim.x) part += s.act_len[sh.list[p][kSoloCap - 1 - i]];
+    part = warp_sum_i(part);
+    if (lane == 0 && part) atomicAdd(&sh.bound, part);
+    if (tid == 0) {
+      int stop = 0;
+      if (nn + nw == 0 || k >= a.max_iter || nn + nw > kSoloLive) stop = 1;
+      if (sh.bound > kSoloCap || sh.seen_n + sh.bound > kSoloSeen / 2) stop = 1;
+      if (((k - k0) & 31) == 31 && global_timer_ns() - t0 > kSoloBudgetNs) stop = 1;
+      sh.stop = stop;
+    }
+    for (int i = tid; i < kSoloHash; i += blockDim.x) sh.hash[i] = -1;
+    if (tid == 0) {
+      sh.cnt[p ^ 1][0] = 0;
+      sh.cnt[p ^ 1][1] = 0;
+    }
+    __syncthreads();
+    if (sh.stop) break;
+    if (tid == 0 && a.record && k < kRecordIters) s.rec_fsizes[k] = nn + nw;
+    const float *src = ((cb ^ k) & 1) ? s.lab1 : s.lab0;
+    float *dst = ((cb ^ k) & 1) ? s.lab0 : s.lab1;
+    int *next = sh.list[p ^ 1];
+    auto mark = [&](bool cand, int v) {
+      if (!cand || !shared_insert(sh.hash, kSoloHash, v)) return;
+      if (s.act_len[v] > kNarrowMax) next[kSoloCap - 1 - atomicAdd(&sh.cnt[p ^ 1][1], 1)] = v;
+      else next[atomicAdd(&sh.cnt[p ^ 1][0], 1)] = v;
+      if (shared_insert(sh.seen, kSoloSeen, v)) atomicAdd(&sh.seen_n, 1);
+    };
+    for (int base = warp * GPW; base < nn; base += (blockDim.x >> 5) * GPW) {
+      const int item = base + grp;
+      const bool valid = item < nn;
+      narrow_row<G>(s, src, dst, a.delta, valid ? sh.list[p][item] : 0, valid, gl, edges, visits, mark);
+    }
+    for (int wi = warp; wi < nw; wi += blockDim.x >> 5)
+      wide_row(s, src, dst, a.delta, sh.list[p][kSoloCap - 1 - wi], lane, edges, visits, mark);
+    __syncthreads();
+  }
+  // hand F_k back to the grid: global set k%3, empty set (k+1)%3
+  {
+    const int set = k % 3;
+    const int nn = sh.cnt[p][0], nw = sh.cnt[p][1];
+    int *gl_list = s.flist + static_cast<size_t>(set) * n;
+    for (int i = tid; i < nn; i += blockDim.x) gl_list[i] = sh.list[p][i];
+    for (int i = tid; i < nw; i += blockDim.x) gl_list[n - 1 - i] = sh.list[p][kSoloCap - 1 - i];
+    if (tid == 0) {
+      s.bc->front_count[set][0] = nn;
+      s.bc->front_count[set][1] = nw;
+      s.bc->front_count[(k + 1) % 3][0] = 0;
+      s.bc->front_count[(k + 1) % 3][1] = 0;
+      s.bc->solo_k = k;
+      s.bc->solo_passes = k - k0;
+    }
+    // vertices that first entered a frontier in solo mode join the touched
+    // list; their stamps stay below the next grid pass's stamp
+    const unsigned st = w.g0 + static_cast<unsigned>(k);
+    int *tl = s.touched + static_cast<size_t>(a.seq & 1) * n;
+    for (int i = tid; i < kSoloSeen; i += blockDim.x) {
+      const int v = sh.seen[i];
+      if (v < 0) continue;
+      const unsigned old = atomicMax(&s.front_stamp[v], st);
+      if (old < w.g0) tl[atomicAdd(&s.ctl->touched_count[a.seq & 1], 1)] = v;
+    }
+  }
+  return k;
+}
+
+template <int G>
+__device__ bool phase_g(const View &w, const Ctx &c, int &iterations, unsigned long long &edges,
+                        unsigned long long &visits, SoloShared &solo) {
+  const DevState &s = w.s;
+  const BatchArgs &a = w.a;
+  const int n = s.n;
   constexpr int GPW = 32 / G;
   const int grp = c.lane / G;
   const int gl = c.lane & (G - 1);
   const int cb = s.ctl->cur_buf;
   int k = 0;
+  int no_solo_at = -1;  // a pass solo mode declined to run goes to the grid
   for (;; ++k) {
     const int set = k % 3;
     const int nn = ld_relaxed_i32(&s.bc->front_count[set][0]);
     const int nw = ld_relaxed_i32(&s.bc->front_count[set][1]);
     if (nn + nw == 0 || k >= a.max_iter) break;
+    if (a.solo && nn + nw <= kSoloEntry && k != no_solo_at) {
+      if (blockIdx.x == 0) solo_passes<G>(w, k, solo, edges, visits);
+      if (!grid_sync(&s.ctl->bar, &s.ctl->err, a.timeout_ns)) return false;
+      const int done = ld_relaxed_i32(&s.bc->solo_passes);
+      const int kk = ld_relaxed_i32(&s.bc->solo_k);
+      if (done == 0) no_solo_at = k;
+      k = kk - 1;  // the loop increment resumes at pass kk
+      continue;
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       // the set filled two passes from now was last read one pass ago
       s.bc->front_count[(k + 2) % 3][0] = 0;
@@ -532,7 +810,6 @@ __device__ bool phase_g(const View &w, const Ctx &c, int &iterations, unsigned l
     const unsigned stamp = w.g0 + static_cast<unsigned>(k) + 1u;
     const int nset = (k + 1) % 3;
     const int *cur_list = s.flist + static_cast<size_t>(set) * n;
-
     auto mark = [&](bool cand, int v) {
       bool fresh = false, first = false;
       if (cand) {
@@ -542,122 +819,13 @@ __device__ bool phase_g(const View &w, const Ctx &c, int &iterations, unsigned l
       }
       frontier_append(w, fresh, first, v, nset);
     };
-
-    // rows of at most 32 entries: groups of G lanes
     for (int base = c.gwarp * GPW; base < nn; base += c.nwarps * GPW) {
       const int item = base + grp;
       const bool valid = item < nn;
-      int u = 0, rs = 0, len = 0;
-      if (valid) {
-        u = cur_list[item];
-        rs = s.full_row[u];
-        len = s.act_len[u];
-      }
-      float sw[R], sl[R];
-      int vv[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int e = gl + G * r;
-        sw[r] = 0.0f;
-        sl[r] = 0.0f;
-        vv[r] = -1;
-        if (e < len) {
-          const int2 ent = s.act_adj[rs + e];
-          vv[r] = ent.x;
-          if (ent.x >= 0) {
-            const float wt = __int_as_float(ent.y);
-            sw[r] = wt;
-            sl[r] = __fmaf_rn(wt, src[ent.x], 0.0f);
-          }
-        }
-      }
-#pragma unroll
-      for (int half = R / 2; half >= 1; half >>= 1)
-#pragma unroll
-        for (int r = 0; r < half; ++r) {
-          sw[r] = sw[r] + sw[r + half];
-          sl[r] = sl[r] + sl[r + half];
-        }
-      float tw = sw[0], tl = sl[0];
-#pragma unroll
-      for (int o = G / 2; o >= 1; o >>= 1) {
-        tw = tw + __shfl_down_sync(0xffffffffu, tw, o, G);
-        tl = tl + __shfl_down_sync(0xffffffffu, tl, o, G);
-      }
-      int changed = 0;
-      if (valid && gl == 0) {
-        const float old = src[u];
-        const float nl = updated_label(tw, tl, old);
-        dst[u] = nl;
-        changed = fabsf(nl - old) > a.delta;
-        edges += static_cast<unsigned long long>(len);
-        visits += 1ull;
-      }
-      changed = __shfl_sync(0xffffffffu, changed, 0, G);
-      // changed vertex: non-deleted, non-GT neighbours and itself
-      // (src/iterativePropagation.cu:200-216)
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int v = vv[r];
-        mark(changed && v >= 0 && s.gt[v] < 0, v);
-      }
-      mark(changed && gl == 0, u);
+      narrow_row<G>(s, src, dst, a.delta, valid ? cur_list[item] : 0, valid, gl, edges, visits, mark);
     }
-
-    // longer rows: one warp each, 256 slots as lane + 32*j
-    for (int wi = c.gwarp; wi < nw; wi += c.nwarps) {
-      const int u = cur_list[n - 1 - wi];
-      const int rs = s.full_row[u];
-      const int len = s.act_len[u];
-      float sw[8], sl[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) sw[j] = sl[j] = 0.0f;
-      for (int p = 0; p < len; p += 256) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int e = p + j * 32 + c.lane;
-          if (e < len) {
-            const int2 ent = s.act_adj[rs + e];
-            if (ent.x >= 0) {
-              const float wt = __int_as_float(ent.y);
-              sw[j] = sw[j] + wt;
-              sl[j] = __fmaf_rn(wt, src[ent.x], sl[j]);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int half = 4; half >= 1; half >>= 1)
-#pragma unroll
-        for (int j = 0; j < half; ++j) {
-          sw[j] = sw[j] + sw[j + half];
-          sl[j] = sl[j] + sl[j + half];
-        }
-      float tw = sw[0], tl = sl[0];
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) {
-        tw = tw + __shfl_down_sync(0xffffffffu, tw, o);
-        tl = tl + __shfl_down_sync(0xffffffffu, tl, o);
-      }
-      int changed = 0;
-      if (c.lane == 0) {
-        const float old = src[u];
-        const float nl = updated_label(tw, tl, old);
-        dst[u] = nl;
-        changed = fabsf(nl - old) > a.delta;
-        edges += static_cast<unsigned long long>(len);
-        visits += 1ull;
-      }
-      changed = __shfl_sync(0xffffffffu, changed, 0);
-      if (changed) {
-        for (int e0 = 0; e0 < len; e0 += 32) {
-          const int e = e0 + c.lane;
-          const int v = e < len ? s.act_adj[rs + e].x : -1;
-          mark(v >= 0 && s.gt[v] < 0, v);
-        }
-        mark(c.lane == 0, u);
-      }
-    }
+    for (int wi = c.gwarp; wi < nw; wi += c.nwarps)
+      wide_row(s, src, dst, a.delta, cur_list[n - 1 - wi], c.lane, edges, visits, mark);
     if (!grid_sync(&s.ctl->bar, &s.ctl->err, a.timeout_ns)) return false;
   }
   iterations = k;
@@ -769,7 +937,8 @@ __global__ void __launch_bounds__(kBlock) batch_kernel(DevState s, BatchArgs a) 
 
   int iterations = 0;
   unsigned long long edges = 0, visits = 0;
-  if (!phase_g<G>(w, c, iterations, edges, visits)) return;
+  __shared__ SoloShared solo;
+  if (!phase_g<G>(w, c, iterations, edges, visits, solo)) return;
   const int new_buf = s.ctl->cur_buf ^ (iterations & 1);
   phase_h(w, c, new_buf);
   edges = static_cast<unsigned long long>(warp_sum_ll(static_cast<long long>(edges)));

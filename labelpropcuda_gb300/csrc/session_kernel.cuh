@@ -35,6 +35,8 @@ struct BatchCounters {
   int num_comp;
   int seed_frontier;
   int hook_rounds;
+  int solo_k;             // pass at which the last solo stint handed back
+  int solo_passes;        // passes that stint ran
   int hook_flag[kMaxHookRounds];
   unsigned long long aff_edges;
   unsigned long long front_visits;
@@ -108,6 +110,7 @@ struct BatchArgs {
   int max_iter;
   int spec;
   int record;
+  int solo;                 // small frontiers run on one block (see phase G)
   unsigned long long timeout_ns;
 };
 

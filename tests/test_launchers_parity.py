@@ -37,16 +37,11 @@ def replay(oracle, p, nb=None):
     gt = np.full(n, -1, np.int32)
     labels = np.full(n, 0.5, np.float32)
     m_full = p.num_edges
-    d_row = DeviceArray(nbytes=4 * (n + 1))
-    d_col = DeviceArray(nbytes=4 * max(m_full, 1))
-    d_val = DeviceArray(nbytes=4 * max(m_full, 1))
-    d_lab = DeviceArray(nbytes=4 * n)
-    d_buf = DeviceArray(nbytes=4 * n)
-    d_st = DeviceArray(nbytes=4 * n)
-    d_gt = DeviceArray(nbytes=4 * n)
-    d_aff = DeviceArray(nbytes=4 * n)
-    d_comp = DeviceArray(nbytes=4 * n)
-    d_new = DeviceArray(nbytes=4 * n)
+    i32 = lambda c: DeviceArray(dtype=np.int32, count=max(c, 1))
+    f32 = lambda c: DeviceArray(dtype=np.float32, count=max(c, 1))
+    d_row, d_col, d_val = i32(n + 1), i32(m_full), f32(m_full)
+    d_lab, d_buf = f32(n), f32(n)
+    d_st, d_gt, d_aff, d_comp, d_new = i32(n), i32(n), i32(n), i32(n), i32(n)
     L.dlp_memset(d_comp.ptr, 0xFF, 4 * n)
     batches = p.batches if nb is None else p.batches[:nb]
     for b, bt in enumerate(batches):
@@ -80,9 +75,7 @@ def replay(oracle, p, nb=None):
         if I and E:
             es, ed, ew, ins = DeviceArray(bt.edge_src), DeviceArray(bt.edge_dst), DeviceArray(bt.edge_weight), \
                 DeviceArray(bt.inserted)
-            sub_col = DeviceArray(nbytes=4 * max(2 * E, 1))
-            sub_val = DeviceArray(nbytes=4 * max(2 * E, 1))
-            sub_row = DeviceArray(nbytes=4 * (I + 1))
+            sub_col, sub_val, sub_row = i32(2 * E), f32(2 * E), i32(I + 1)
             nsn, nse = ctypes.c_int(0), ctypes.c_int(0)
             N.check(L.dlp_build_sparsified_subgraph(d_row.ptr, d_col.ptr, d_val.ptr, d_aff.ptr, d_st.ptr, es.ptr,
                                                     ed.ptr, ew.ptr, E, ins.ptr, I, d_new.ptr, float(tau), sub_row.ptr,
