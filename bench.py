@@ -245,7 +245,11 @@ def gpu_arm(args, td, rank, world, local_rank):
         flush_l2()
         for b in range(nb):
             sess.apply_device(b, dev_batches[b])
-        sess.synchronize()
+        try:
+            sess.synchronize()
+        except dlp.DlpError:
+            print("device diagnostics:", sess.debug(), file=sys.stderr, flush=True)
+            raise
         stats = [sess.stats(b) for b in range(nb)]
         return sess.elapsed_ms(0, nb - 1), stats
 

@@ -107,6 +107,10 @@ typedef struct dlp_config {
   int narrow_lanes;      /* lanes per short row in propagation: 4, 8, 16 or 32; 0 = tuned */
   int blocks_per_sm;     /* persistent grid occupancy; 0 = from the occupancy query */
   double wait_timeout_s; /* limit for any device-side wait; <= 0: 2 s */
+  int small_frontier_solo; /* bit 0: passes over small frontiers run on one
+                              thread block with block barriers; bit 1: passes
+                              over mid-size frontiers run on a sub-grid with its
+                              own barrier. Default 3 (both); same results. */
 } dlp_config;
 
 void dlp_config_default(dlp_config *cfg);
@@ -166,6 +170,8 @@ void *dlp_session_stream(dlp_session *s);
  * end of the latest application of batch `last` (CUDA events on the session
  * stream); waits for the stream. */
 int dlp_session_elapsed_ms(dlp_session *s, int first, int last, float *ms);
+/* Device-side diagnostics after a failed batch (see dlp_engine_debug). */
+int dlp_session_debug(dlp_session *s, int *out4);
 
 /* Artefacts of the last applied batch when cfg.record != 0 (4-byte elements;
  * *count receives the element count; host_out may be NULL to query it). */
@@ -181,6 +187,53 @@ enum dlp_artefact {
 };
 int dlp_session_artefact(dlp_session *s, int which, void *host_out, int64_t capacity,
                          int64_t *count);
+
+/* ------------------------------------------------------------------------ */
+/* 2b. Batch engine: many resident graphs; one step applies one batch to     */
+/*     each of several graphs in ONE cooperative launch (flattened work      */
+/*     lists, per-graph convergence). A session is a one-graph engine.       */
+/* ------------------------------------------------------------------------ */
+
+typedef struct dlp_engine dlp_engine;
+
+/* max_graphs <= 1024; memory_budget_bytes = 0 means no budget. */
+int dlp_engine_create(const dlp_config *cfg, int max_graphs, size_t memory_budget_bytes, dlp_engine **out);
+int dlp_engine_destroy(dlp_engine *e);
+/* Device bytes a graph of this size occupies once added (admission). */
+size_t dlp_engine_graph_bytes(int num_nodes, int64_t num_edges, int with_truth, int with_batch_map, int record);
+size_t dlp_engine_bytes_in_use(const dlp_engine *e);
+/* Uploads a graph (same arrays as dlp_session_create); fails with
+ * DLP_ERR_OUT_OF_MEMORY when it would exceed the budget. */
+int dlp_engine_add_graph(dlp_engine *e, int num_nodes, int64_t num_edges, const int *row_ptr,
+                         const int *col_ind, const float *values, const float *true_labels,
+                         const int *vertex_batch_map, int *graph_id);
+/* Frees a graph's device memory (eviction); its id becomes free. */
+int dlp_engine_remove_graph(dlp_engine *e, int graph_id);
+int dlp_engine_reset_graph(dlp_engine *e, int graph_id);
+float dlp_engine_tau(const dlp_engine *e, int graph_id);
+void *dlp_engine_stream(dlp_engine *e);
+/* One step over `count` distinct graphs: batch i (host arrays) is applied to
+ * graph_ids[i] as its batch batch_indices[i]. With stats != NULL the call
+ * waits and fills stats[i]. */
+int dlp_engine_step(dlp_engine *e, int count, const int *graph_ids, const int *batch_indices,
+                    const dlp_batch_view *host_batches, dlp_batch_stats *stats);
+/* Same with device-resident batch arrays (they need not outlive the step);
+ * never waits. */
+int dlp_engine_step_device(dlp_engine *e, int count, const int *graph_ids, const int *batch_indices,
+                           const dlp_batch_view *device_batches);
+int dlp_engine_synchronize(dlp_engine *e);
+int dlp_engine_stats(dlp_engine *e, int graph_id, int batch_index, dlp_batch_stats *out);
+/* Steps launched so far, and the device time from the start of step `first`
+ * to the end of step `last`. */
+int dlp_engine_steps(const dlp_engine *e);
+/* Device-side diagnostics after a failed step: out[0] error code, out[1] last
+ * phase reached (1..10), out[2] last propagation pass started, out[3] passes
+ * of the last one-block / sub-grid stint. */
+int dlp_engine_debug(dlp_engine *e, int *out4);
+int dlp_engine_elapsed_ms(dlp_engine *e, int first_step, int last_step, float *ms);
+int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels);
+int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, int64_t capacity,
+                        int64_t *count);
 
 /* ------------------------------------------------------------------------ */
 /* 3. Step launchers on caller-owned device arrays, reference layout.        */

@@ -117,14 +117,14 @@ class Session:
     def __init__(self, num_nodes: int, row_ptr, col_ind, values, true_labels=None, vertex_batch_map=None, *,
                  tau: float = -1.0, delta: float = 1e-4, max_iterations: int = 100000,
                  semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False, narrow_lanes: int = 0,
-                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: bool = True):
+                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: int = 3):
         L = _n.lib()
         cfg = _n.Config()
         L.dlp_config_default(ctypes.byref(cfg))
         cfg.tau, cfg.delta, cfg.max_iterations = tau, delta, max_iterations
         cfg.semantics, cfg.device, cfg.record = semantics, device, int(bool(record))
         cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
-        cfg.small_frontier_solo = int(bool(small_frontier_solo))
+        cfg.small_frontier_solo = int(small_frontier_solo)
         self._keep = [np.ascontiguousarray(row_ptr, dtype=np.int32), np.ascontiguousarray(col_ind, dtype=np.int32),
                       np.ascontiguousarray(values, dtype=np.float32)]
         tl = None if true_labels is None else np.ascontiguousarray(true_labels, dtype=np.float32)
@@ -190,6 +190,11 @@ class Session:
         _n.check(_n.lib().dlp_session_elapsed_ms(self._h, first, last, ctypes.byref(ms)))
         return float(ms.value)
 
+    def debug(self) -> dict:
+        out = (ctypes.c_int * 4)()
+        _n.check(_n.lib().dlp_session_debug(self._h, out))
+        return {"err": out[0], "phase": out[1], "pass": out[2], "small_passes": out[3]}
+
     def labels(self) -> np.ndarray:
         out = np.empty(self.num_nodes, dtype=np.float32)
         _n.check(_n.lib().dlp_session_read_labels(self._h, out.ctypes.data))
@@ -203,6 +208,117 @@ class Session:
         if cnt.value:
             _n.check(_n.lib().dlp_session_artefact(self._h, which, out.ctypes.data, cnt.value, ctypes.byref(cnt)))
         return out
+
+
+class Engine:
+    """Many resident graphs; step() applies one batch to each of several graphs
+    in one cooperative launch (dlp_engine_*)."""
+
+    def __init__(self, max_graphs: int, memory_budget_bytes: int = 0, *, tau: float = -1.0, delta: float = 1e-4,
+                 max_iterations: int = 100000, semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False,
+                 narrow_lanes: int = 0, blocks_per_sm: int = 0, wait_timeout_s: float = 2.0,
+                 small_frontier_solo: int = 3):
+        L = _n.lib()
+        cfg = _n.Config()
+        L.dlp_config_default(ctypes.byref(cfg))
+        cfg.tau, cfg.delta, cfg.max_iterations = tau, delta, max_iterations
+        cfg.semantics, cfg.device, cfg.record = semantics, device, int(bool(record))
+        cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
+        cfg.small_frontier_solo = int(small_frontier_solo)
+        self._h = ctypes.c_void_p()
+        _n.check(L.dlp_engine_create(ctypes.byref(cfg), max_graphs, memory_budget_bytes, ctypes.byref(self._h)))
+        self.sizes: dict[int, int] = {}
+
+    @staticmethod
+    def graph_bytes(num_nodes: int, num_edges: int, truth: bool = True, batch_map: bool = True,
+                    record: bool = False) -> int:
+        return int(_n.lib().dlp_engine_graph_bytes(num_nodes, num_edges, int(truth), int(batch_map), int(record)))
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(_n.lib().dlp_engine_bytes_in_use(self._h))
+
+    def add_graph(self, num_nodes, row_ptr, col_ind, values, true_labels=None, vertex_batch_map=None) -> int:
+        keep = [np.ascontiguousarray(row_ptr, dtype=np.int32), np.ascontiguousarray(col_ind, dtype=np.int32),
+                np.ascontiguousarray(values, dtype=np.float32)]
+        tl = None if true_labels is None else np.ascontiguousarray(true_labels, dtype=np.float32)
+        bm = None if vertex_batch_map is None else np.ascontiguousarray(vertex_batch_map, dtype=np.int32)
+        gid = ctypes.c_int(-1)
+        _n.check(_n.lib().dlp_engine_add_graph(self._h, num_nodes, keep[1].size, keep[0].ctypes.data, _ptr(keep[1]),
+                                               _ptr(keep[2]), _ptr(tl), _ptr(bm), ctypes.byref(gid)))
+        self.sizes[gid.value] = num_nodes
+        return gid.value
+
+    def add_problem(self, p: Problem) -> int:
+        return self.add_graph(p.num_nodes, p.row_ptr, p.col_ind, p.values, p.true_labels, p.batch_map())
+
+    def remove_graph(self, gid: int) -> None:
+        _n.check(_n.lib().dlp_engine_remove_graph(self._h, gid))
+        self.sizes.pop(gid, None)
+
+    def reset_graph(self, gid: int) -> None:
+        _n.check(_n.lib().dlp_engine_reset_graph(self._h, gid))
+
+    def tau(self, gid: int) -> float:
+        return float(_n.lib().dlp_engine_tau(self._h, gid))
+
+    def step(self, items: list[tuple[int, int, "Batch"]], wait: bool = True):
+        """items: (graph id, batch index, Batch with host arrays)."""
+        n = len(items)
+        gids = (ctypes.c_int * n)(*[g for g, _, _ in items])
+        bidx = (ctypes.c_int * n)(*[b for _, b, _ in items])
+        views = (_n.BatchView * n)(*[bt.view() for _, _, bt in items])
+        if wait:
+            stats = (_n.BatchStats * n)()
+            _n.check(_n.lib().dlp_engine_step(self._h, n, gids, bidx, views, stats))
+            return [s.as_dict() for s in stats]
+        _n.check(_n.lib().dlp_engine_step(self._h, n, gids, bidx, views, None))
+        return None
+
+    def step_device(self, items: list[tuple[int, int, "DeviceBatch"]]) -> None:
+        n = len(items)
+        gids = (ctypes.c_int * n)(*[g for g, _, _ in items])
+        bidx = (ctypes.c_int * n)(*[b for _, b, _ in items])
+        views = (_n.BatchView * n)(*[db if isinstance(db, _n.BatchView) else db.view() for _, _, db in items])
+        _n.check(_n.lib().dlp_engine_step_device(self._h, n, gids, bidx, views))
+
+    def synchronize(self) -> None:
+        _n.check(_n.lib().dlp_engine_synchronize(self._h))
+
+    def stats(self, gid: int, batch_index: int) -> dict:
+        st = _n.BatchStats()
+        _n.check(_n.lib().dlp_engine_stats(self._h, gid, batch_index, ctypes.byref(st)))
+        return st.as_dict()
+
+    def debug(self) -> dict:
+        out = (ctypes.c_int * 4)()
+        _n.check(_n.lib().dlp_engine_debug(self._h, out))
+        return {"err": out[0], "phase": out[1], "pass": out[2], "small_passes": out[3]}
+
+    @property
+    def steps(self) -> int:
+        return int(_n.lib().dlp_engine_steps(self._h))
+
+    def elapsed_ms(self, first_step: int, last_step: int) -> float:
+        ms = ctypes.c_float(0.0)
+        _n.check(_n.lib().dlp_engine_elapsed_ms(self._h, first_step, last_step, ctypes.byref(ms)))
+        return float(ms.value)
+
+    def labels(self, gid: int) -> np.ndarray:
+        out = np.empty(self.sizes[gid], dtype=np.float32)
+        _n.check(_n.lib().dlp_engine_read_labels(self._h, gid, out.ctypes.data))
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            _n.lib().dlp_engine_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class DeviceArray:
@@ -251,6 +367,40 @@ class DeviceArray:
             self.free()
         except Exception:
             pass
+
+
+class PackedBatches:
+    """Many batches uploaded to one device buffer with one copy (16-byte
+    aligned segments); view(i) is the device view of batch i."""
+
+    def __init__(self, batches: list[Batch]):
+        parts, offs = [], []
+        off = 0
+        for bt in batches:
+            o = []
+            for a in (bt.inserted, bt.gt_ids, bt.gt_labels, bt.deleted, bt.edge_src, bt.edge_dst, bt.edge_weight):
+                o.append(off)
+                parts.append((off, a))
+                off += (a.nbytes + 15) & ~15
+            offs.append(o)
+        host = np.zeros(max(off, 16), dtype=np.uint8)
+        for o, a in parts:
+            if a.nbytes:
+                host[o:o + a.nbytes] = np.frombuffer(np.ascontiguousarray(a).tobytes(), dtype=np.uint8)
+        self.buf = DeviceArray(host)
+        self.offs = offs
+        self.sizes = [(bt.inserted.size, bt.gt_ids.size, bt.deleted.size, bt.edge_src.size) for bt in batches]
+
+    def view(self, i: int) -> _n.BatchView:
+        base = self.buf.addr
+        o = [base + x for x in self.offs[i]]
+        ni, ng, nd, ne = self.sizes[i]
+        v = _n.BatchView()
+        v.inserted, v.num_inserted = o[0], ni
+        v.gt_ids, v.gt_labels, v.num_gt = o[1], o[2], ng
+        v.deleted, v.num_deleted = o[3], nd
+        v.edge_src, v.edge_dst, v.edge_weight, v.num_edges = o[4], o[5], o[6], ne
+        return v
 
 
 class DeviceBatch:

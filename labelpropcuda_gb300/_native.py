@@ -107,6 +107,25 @@ _SIGNATURES = {
     "dlp_session_elapsed_ms": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "dlp_irlp": (_I, [_P, _P, _P, _P, _P, _P, _I, ctypes.c_float, _I, c_int_p, _P]),
     "dlp_session_artefact": (_I, [_P, _I, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
+    "dlp_engine_create": (_I, [ctypes.POINTER(Config), _I, ctypes.c_size_t, ctypes.POINTER(_P)]),
+    "dlp_engine_destroy": (_I, [_P]),
+    "dlp_engine_graph_bytes": (ctypes.c_size_t, [_I, ctypes.c_int64, _I, _I, _I]),
+    "dlp_engine_bytes_in_use": (ctypes.c_size_t, [_P]),
+    "dlp_engine_add_graph": (_I, [_P, _I, ctypes.c_int64, _P, _P, _P, _P, _P, c_int_p]),
+    "dlp_engine_remove_graph": (_I, [_P, _I]),
+    "dlp_engine_reset_graph": (_I, [_P, _I]),
+    "dlp_engine_tau": (ctypes.c_float, [_P, _I]),
+    "dlp_engine_stream": (_P, [_P]),
+    "dlp_engine_step": (_I, [_P, _I, _P, _P, ctypes.POINTER(BatchView), ctypes.POINTER(BatchStats)]),
+    "dlp_engine_step_device": (_I, [_P, _I, _P, _P, ctypes.POINTER(BatchView)]),
+    "dlp_engine_synchronize": (_I, [_P]),
+    "dlp_engine_stats": (_I, [_P, _I, _I, ctypes.POINTER(BatchStats)]),
+    "dlp_engine_steps": (_I, [_P]),
+    "dlp_engine_debug": (_I, [_P, c_int_p]),
+    "dlp_session_debug": (_I, [_P, c_int_p]),
+    "dlp_engine_elapsed_ms": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
+    "dlp_engine_read_labels": (_I, [_P, _I, _P]),
+    "dlp_engine_artefact": (_I, [_P, _I, _I, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
     "dlp_mark_deletions": (_I, [_P, _P, _P, _P, _P, _I, _I, _P]),
     "dlp_build_sparsified_subgraph": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _P, ctypes.c_float,
                                            _P, _P, _P, c_int_p, c_int_p, _P]),

@@ -71,25 +71,42 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
   return t;
 }
 
-// Grid-wide barrier for a cooperative launch (all blocks co-resident). The
-// last block to arrive advances the generation; the others wait for it with a
-// time limit. A block that runs out of time records DLP_ERR_TIMEOUT in *err
-// and every block leaves at its next barrier, so no wait is unbounded.
+// Barrier over the first `nblocks` blocks of a cooperative launch (all blocks
+// co-resident). Arrivals are counted in two levels — groups of 16 blocks, then
+// the groups — so they do not all serialise on one counter; the last block to
+// arrive advances the generation, the others wait for it with a time limit. A
+// block that runs out of time records DLP_ERR_TIMEOUT in *err and every block
+// leaves at its next barrier, so no wait is unbounded.
+constexpr int kBarrierGroup = 16;
+constexpr int kBarrierMaxGroups = 128;
+
 struct GridBarrier {
   unsigned count;
   unsigned gen;
+  unsigned group[kBarrierMaxGroups];
 };
 
-__device__ __forceinline__ bool grid_sync(GridBarrier *bar, int *err, uint64_t timeout_ns) {
+__device__ __forceinline__ bool grid_sync_n(GridBarrier *bar, unsigned nblocks, int *err, uint64_t timeout_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
     const unsigned gen = ld_acquire_u32(&bar->gen);
-    const unsigned arrived = atom_add_acq_rel_u32(&bar->count, 1u);
+    const unsigned ngroups = (nblocks + kBarrierGroup - 1) / kBarrierGroup;
+    bool last = false;
+    if (ngroups <= 1 || ngroups > kBarrierMaxGroups) {
+      last = atom_add_acq_rel_u32(&bar->count, 1u) == nblocks - 1;
+      if (last) bar->count = 0;
+    } else {
+      const unsigned grp = blockIdx.x / kBarrierGroup;
+      const unsigned gsize = min(static_cast<unsigned>(kBarrierGroup), nblocks - grp * kBarrierGroup);
+      if (atom_add_acq_rel_u32(&bar->group[grp], 1u) == gsize - 1) {
+        bar->group[grp] = 0;  // ordered before the release of the next arrival
+        last = atom_add_acq_rel_u32(&bar->count, 1u) == ngroups - 1;
+        if (last) bar->count = 0;
+      }
+    }
     int ok = 1;
-    if (arrived == nblocks - 1) {
-      bar->count = 0;
+    if (last) {
       st_release_u32(&bar->gen, gen + 1);
     } else {
       const uint64_t t0 = global_timer_ns();
@@ -107,6 +124,10 @@ __device__ __forceinline__ bool grid_sync(GridBarrier *bar, int *err, uint64_t t
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_sync(GridBarrier *bar, int *err, uint64_t timeout_ns) {
+  return grid_sync_n(bar, gridDim.x * gridDim.y * gridDim.z, err, timeout_ns);
 }
 
 // Appends the set lanes' values to list[*count ...] with one atomic per warp.

@@ -20,7 +20,7 @@
 namespace dlp {
 namespace session {
 
-constexpr int kBlock = 256;
+constexpr int kBlock = 512;
 constexpr int kMaxHookRounds = 100;     // the reference's outer SV cap (src/connectedComponents.cu:209)
 constexpr int kRecordIters = 1 << 17;   // per-pass frontier sizes kept when recording
 constexpr int kNarrowMax = 32;          // rows up to this length use the group path
@@ -35,8 +35,7 @@ struct BatchCounters {
   int num_comp;
   int seed_frontier;
   int hook_rounds;
-  int solo_k;             // pass at which the last solo stint handed back
-  int solo_passes;        // passes that stint ran
+  int passes;             // propagation passes this graph ran
   int hook_flag[kMaxHookRounds];
   unsigned long long aff_edges;
   unsigned long long front_visits;
@@ -78,6 +77,7 @@ struct DevState {
   int *sub_pairs;           // kept edges: (src,dst) global ids
   int *sub_local;           // kept edges: (src,dst) inserted positions
   int *del_pre;             // spec: status before the batch, per deleted entry
+  int *del_keep;            // this batch's deletions, read by the next batch
   SessionCtl *ctl;
   BatchCounters *bc;
   dlp_batch_stats *stats_slot;

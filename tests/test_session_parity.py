@@ -63,6 +63,20 @@ def test_session_matches_oracle(gpu, oracle, cfg):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("sem", [dlp.SEMANTICS_REF, dlp.SEMANTICS_SPEC])
+def test_solo_mode_gives_identical_results(gpu, sem):
+    """Small frontiers on one block (default) vs every pass on the whole grid."""
+    p = dlp.Problem(5000, 5, 10, 42)
+    a = dlp.Session.from_problem(p, semantics=sem, small_frontier_solo=True)
+    b = dlp.Session.from_problem(p, semantics=sem, small_frontier_solo=False)
+    for i, bt in enumerate(p.batches):
+        sa, sb = a.apply(i, bt), b.apply(i, bt)
+        for k in EXACT_STATS:
+            assert sa[k] == sb[k], (i, k)
+        assert a.labels().tobytes() == b.labels().tobytes(), i
+
+
+@pytest.mark.gpu
 def test_reset_replays_identically(gpu):
     p = dlp.Problem(5000, 5, 10, 42)
     sess = dlp.Session.from_problem(p)
