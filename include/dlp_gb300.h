@@ -276,6 +276,22 @@ int dlp_iterative_propagation(const int *d_row_ptr, const int *d_col_ind, const 
                               float delta, int max_iterations, int *iterations_used,
                               void *stream);
 
+/* Same arguments and results as dlp_iterative_propagation, but allocates no
+ * device memory: its scratch is a fixed array inside this library (16 MiB +
+ * 1 KiB, present on every GPU that loads the library until the process ends).
+ * No counterpart in the reference, whose launchers call cudaMalloc/cudaFree on
+ * every call. For callers that may not allocate device memory while running:
+ * hosts that own the device's whole memory pool, or services that reserve all
+ * memory up front so that nothing can fail or stall later. Limits and rules:
+ * num_nodes <= 1048576 (larger graphs get DLP_ERR_INVALID_ARGUMENT); the first
+ * call on a device looks up the array's address, so make it before any stream
+ * capture; every call reuses the same array, so calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int dlp_iterative_propagation_noalloc(const int *d_row_ptr, const int *d_col_ind, const float *d_values,
+                                      float *d_labels, float *d_labels_buffer, const int *d_vertex_status,
+                                      const int *d_gt_class, int *d_is_affected, int num_nodes, float delta,
+                                      int max_iterations, int *iterations_used, void *stream);
+
 /* launchIrLP (src/validation.cu:145-208): full recompute of every active
  * non-ground-truth vertex per iteration until no label moves by more than
  * delta, as one cooperative launch. Result in d_labels. */

@@ -132,6 +132,8 @@ _SIGNATURES = {
     "dlp_connected_components": (_I, [_P, _P, _I, _P, _I, _P, c_int_p, _I, _P]),
     "dlp_label_initialization": (_I, [_P, _P, _P, _P, _P, _P, _I, _P, _I, _P, _I, _P]),
     "dlp_iterative_propagation": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _I, ctypes.c_float, _I, c_int_p, _P]),
+    "dlp_iterative_propagation_noalloc": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _I, ctypes.c_float, _I, c_int_p,
+                                               _P]),
     "dlp_device_count": (_I, [c_int_p]),
     "dlp_set_device": (_I, [_I]),
     "dlp_malloc": (_I, [ctypes.POINTER(_P), ctypes.c_size_t]),

@@ -13,6 +13,7 @@
 // outputs require.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "common.cuh"
 #include "row_sums.cuh"
@@ -601,6 +602,48 @@ int coop_grid(const void *kernel) {
 
 using namespace dlp::ref_layout;
 
+// ---------------------------------------------------------------------------
+// Scratch of dlp_iterative_propagation_noalloc: the frontier stamps, the three
+// frontier lists, the counters and the grid barrier of one propagation call on
+// a graph of at most kNoAllocMaxNodes vertices (16 MiB + 1 KiB). It is a
+// file-scope device array, so it exists on every GPU that loads this library,
+// from module load until the process exits, whether or not the entry point is
+// ever called.
+namespace {
+constexpr int kNoAllocMaxNodes = 1 << 20;
+struct NoAllocScratch {
+  unsigned stamp[kNoAllocMaxNodes];
+  int lists[3 * kNoAllocMaxNodes];
+  int small[16];
+  dlp::GridBarrier bar;
+};
+}  // namespace
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+namespace {
+// The array's device address, looked up once per device (the host-side name
+// of a __device__ variable is not a device address). Fixed table: no heap use.
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+NoAllocScratch *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+int noalloc_scratch(NoAllocScratch **out) {
+  int dev = -1;
+  DLP_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "device ordinal too large");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return dlp::cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    g_noalloc_addr[dev] = static_cast<NoAllocScratch *>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return DLP_OK;
+}
+}  // namespace
+
 extern "C" {
 
 int dlp_mark_deletions(int *d_row_ptr, int *d_col_ind, int *d_vertex_status, int *d_is_affected,
@@ -817,6 +860,72 @@ int dlp_iterative_propagation(const int *d_row_ptr, const int *d_col_ind, const 
   for (void *p : {static_cast<void *>(stamp), static_cast<void *>(lists), static_cast<void *>(small),
                   static_cast<void *>(bar)})
     cudaFreeAsync(p, s);
+  if (host[1]) return dlp::fail(host[1], "propagation failed on the device");
+  *iterations_used = host[0];
+  return DLP_OK;
+}
+
+// dlp_iterative_propagation without any device allocation: the same kernel and
+// results, with its scratch in g_noalloc_scratch instead of cudaMallocAsync
+// temporaries. For callers that must not allocate device memory while they run
+// (a framework that owns the whole device memory pool, a service that reserves
+// its memory at start-up so nothing can fail or stall later). The first call
+// on a device looks the array's address up; make that call before any stream
+// capture. All calls share the one array, so calls that overlap on the GPU
+// (other streams, other host threads) race; serialise them. Graphs of more
+// than 2^20 vertices are rejected.
+int dlp_iterative_propagation_noalloc(const int *d_row_ptr, const int *d_col_ind, const float *d_values,
+                                      float *d_labels, float *d_labels_buffer, const int *d_vertex_status,
+                                      const int *d_gt_class, int *d_is_affected, int num_nodes, float delta,
+                                      int max_iterations, int *iterations_used, void *stream) {
+  dlp::clear_error();
+  if (!iterations_used) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null iterations_used");
+  *iterations_used = 0;
+  if (num_nodes <= 0 || !d_row_ptr || !d_labels || !d_labels_buffer || !d_vertex_status || !d_gt_class ||
+      !d_is_affected)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "invalid arguments to dlp_iterative_propagation_noalloc");
+  if (num_nodes > kNoAllocMaxNodes)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT,
+                     "num_nodes " + std::to_string(num_nodes) + " exceeds the allocation-free limit of " +
+                         std::to_string(kNoAllocMaxNodes) + " vertices; use dlp_iterative_propagation");
+  DLP_TRY(dlp::require_device());
+  NoAllocScratch *sc = nullptr;
+  DLP_TRY(noalloc_scratch(&sc));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = static_cast<size_t>(num_nodes);
+  DLP_CUDA_TRY(cudaMemcpyAsync(d_labels_buffer, d_labels, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  // what must start at zero: the stamps in use, the counters, the barrier
+  DLP_CUDA_TRY(cudaMemsetAsync(sc->stamp, 0, sizeof(unsigned) * n, s));
+  DLP_CUDA_TRY(cudaMemsetAsync(sc->small, 0, sizeof(sc->small), s));
+  DLP_CUDA_TRY(cudaMemsetAsync(&sc->bar, 0, sizeof(sc->bar), s));
+  PropArgs a{};
+  a.row_ptr = d_row_ptr;
+  a.col = d_col_ind;
+  a.val = d_values;
+  a.labels = d_labels;
+  a.buffer = d_labels_buffer;
+  a.status = d_vertex_status;
+  a.gt = d_gt_class;
+  a.affected = d_is_affected;
+  a.n = num_nodes;
+  a.delta = delta;
+  a.max_iter = max_iterations;
+  a.stamp = sc->stamp;
+  a.lists = sc->lists;
+  a.counts = sc->small;
+  a.out = sc->small + 8;
+  a.err = sc->small + 12;
+  a.bar = &sc->bar;
+  a.timeout_ns = 2000000000ull;
+  const void *kern = prop_kernel_ptr(8);
+  const int grid = coop_grid(kern);
+  if (grid <= 0) return dlp::fail(DLP_ERR_CUDA, "occupancy query failed");
+  void *args[] = {&a};
+  DLP_TRY(dlp::launch_cooperative(kern, grid, kBlock, args, 0, s));
+  int host[2] = {0, 0};
+  DLP_CUDA_TRY(cudaMemcpyAsync(&host[0], a.out, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DLP_CUDA_TRY(cudaMemcpyAsync(&host[1], a.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DLP_CUDA_TRY(cudaStreamSynchronize(s));
   if (host[1]) return dlp::fail(host[1], "propagation failed on the device");
   *iterations_used = host[0];
   return DLP_OK;
