@@ -218,7 +218,8 @@ void *dlp_engine_stream(dlp_engine *e);
 int dlp_engine_step(dlp_engine *e, int count, const int *graph_ids, const int *batch_indices,
                     const dlp_batch_view *host_batches, dlp_batch_stats *stats);
 /* Same with device-resident batch arrays (they need not outlive the step);
- * never waits. */
+ * never waits. Neither call takes a graph whose batch is in progress in
+ * sliced steps (section 2c). */
 int dlp_engine_step_device(dlp_engine *e, int count, const int *graph_ids, const int *batch_indices,
                            const dlp_batch_view *device_batches);
 int dlp_engine_synchronize(dlp_engine *e);
@@ -234,6 +235,85 @@ int dlp_engine_elapsed_ms(dlp_engine *e, int first_step, int last_step, float *m
 int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels);
 int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, int64_t capacity,
                         int64_t *count);
+
+/* ------------------------------------------------------------------------ */
+/* 2c. Continuous batching (no counterpart in the reference, which applies   */
+/*     one batch of one graph at a time). A sliced step starts new batches   */
+/*     and continues unfinished ones in ONE launch, for a bounded slice of   */
+/*     propagation; a server admits waiting requests between slices.         */
+/* ------------------------------------------------------------------------ */
+
+/* Starts batch batch_indices[i] on graph_ids[i] (device-resident arrays that
+ * must stay valid until that batch ends) and continues every graph whose batch
+ * is still in progress, in one launch. The phases before propagation always
+ * complete; propagation stops after pass_budget passes (0: no limit) or once
+ * slice_us microseconds have passed since the launch began (0: no limit),
+ * whichever comes first. Waits for the launch. The ids of the graphs whose
+ * batch ended go to finished_ids (room for max_graphs ids), their number to
+ * *num_finished, the number still in progress to *num_continuing (may be
+ * NULL). A graph in progress cannot start another batch; its statistics and
+ * labels become readable when its batch ends. Every result is bit-identical to
+ * the same batches run by unsliced steps. */
+int dlp_engine_step_sliced(dlp_engine *e, int count, const int *graph_ids, const int *batch_indices,
+                           const dlp_batch_view *device_batches, int pass_budget, double slice_us,
+                           int *finished_ids, int *num_finished, int *num_continuing);
+/* Vertex count of a resident graph, -1 for an unknown id. */
+int dlp_engine_graph_nodes(const dlp_engine *e, int graph_id);
+/* 1 while graph_id has a batch in progress in sliced steps, else 0. */
+int dlp_engine_in_progress(const dlp_engine *e, int graph_id);
+
+typedef struct dlp_server dlp_server;
+
+typedef struct {
+  double slice_us;            /* propagation time per step before waiting requests join (default 1000) */
+  int pass_budget;            /* propagation passes per step (default 0: no limit) */
+  size_t memory_budget_bytes; /* admission limit: the engine's resident bytes plus the device bytes of
+                                 running requests (default 0: no limit) */
+  int max_batches_per_step;   /* new batches started per step (default 0: the engine's max_graphs) */
+  int serial;                 /* 1: the plain path, one request at a time run to its end (default 0) */
+} dlp_server_config;
+void dlp_server_config_default(dlp_server_config *cfg);
+
+typedef struct {
+  int graph_id;               /* a graph resident in the server's engine */
+  int batch_index;
+  dlp_batch_view batch;       /* host arrays */
+  double arrival_s;           /* dlp_server_replay only: offset from the start of the replay */
+} dlp_request;
+
+typedef struct {
+  int graph_id;
+  int batch_index;
+  int status;                 /* DLP_OK, or why the request failed */
+  double arrival_s;           /* server clock, seconds */
+  double admit_s;             /* first step the batch took part in */
+  double finish_s;            /* its statistics were read back */
+  int steps;                  /* sliced steps the batch took part in */
+  dlp_batch_stats stats;
+} dlp_request_result;
+
+/* A server drives one engine; graphs are added to the engine beforehand. */
+int dlp_server_create(dlp_engine *e, const dlp_server_config *cfg, dlp_server **out);
+int dlp_server_destroy(dlp_server *s);
+/* Seconds since the server was created (the clock of dlp_request_result). */
+double dlp_server_clock(const dlp_server *s);
+/* Queues a request (its arrays are copied); *request_id identifies it. */
+int dlp_server_submit(dlp_server *s, const dlp_request *req, int *request_id);
+/* One scheduling round: admits queued requests in arrival order (one batch
+ * per graph at a time, within the memory budget), runs one sliced step over
+ * them and the batches in progress, and writes the ids of the requests that
+ * ended (up to capacity). Returns at once when nothing is queued or running. */
+int dlp_server_poll(dlp_server *s, int *completed_ids, int capacity, int *num_completed);
+int dlp_server_result(const dlp_server *s, int request_id, dlp_request_result *out);
+/* Requests queued or running. */
+int dlp_server_pending(const dlp_server *s);
+/* Replays a trace in real time: reqs[i] (sorted by arrival_s) is submitted
+ * once arrival_s seconds have passed since the call began, and the server
+ * polls until every request has ended. out[i] holds request i's result with
+ * times relative to the start of the replay; *makespan_s is the time until
+ * the last one ended. The arrays are used in place during the call. */
+int dlp_server_replay(dlp_server *s, int count, const dlp_request *reqs, dlp_request_result *out,
+                      double *makespan_s);
 
 /* ------------------------------------------------------------------------ */
 /* 3. Step launchers on caller-owned device arrays, reference layout.        */

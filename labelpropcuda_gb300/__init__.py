@@ -282,6 +282,25 @@ class Engine:
         views = (_n.BatchView * n)(*[db if isinstance(db, _n.BatchView) else db.view() for _, _, db in items])
         _n.check(_n.lib().dlp_engine_step_device(self._h, n, gids, bidx, views))
 
+    def step_sliced(self, items: list[tuple[int, int, "DeviceBatch"]], pass_budget: int = 0,
+                    slice_us: float = 0.0) -> tuple[list[int], int]:
+        """Starts the given batches (device arrays that must outlive their batch)
+        and continues every unfinished one, for at most pass_budget passes /
+        slice_us of propagation. Returns (graphs whose batch ended, graphs still
+        in progress)."""
+        n = len(items)
+        gids = (ctypes.c_int * max(n, 1))(*[g for g, _, _ in items])
+        bidx = (ctypes.c_int * max(n, 1))(*[b for _, b, _ in items])
+        views = (_n.BatchView * max(n, 1))(*[db if isinstance(db, _n.BatchView) else db.view() for _, _, db in items])
+        fin = (ctypes.c_int * 1024)()
+        nf, nc = ctypes.c_int(0), ctypes.c_int(0)
+        _n.check(_n.lib().dlp_engine_step_sliced(self._h, n, gids, bidx, views, pass_budget, slice_us, fin,
+                                                 ctypes.byref(nf), ctypes.byref(nc)))
+        return [fin[i] for i in range(nf.value)], nc.value
+
+    def in_progress(self, gid: int) -> bool:
+        return bool(_n.lib().dlp_engine_in_progress(self._h, gid))
+
     def synchronize(self) -> None:
         _n.check(_n.lib().dlp_engine_synchronize(self._h))
 
@@ -319,6 +338,79 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous batching over an Engine (dlp_server_*): requests wait in
+    arrival order; each poll admits what fits and runs one sliced step over the
+    admitted batches and those in progress. serial=True is the plain path."""
+
+    def __init__(self, engine: Engine, *, slice_us: float = 1000.0, pass_budget: int = 0,
+                 memory_budget_bytes: int = 0, max_batches_per_step: int = 0, serial: bool = False):
+        L = _n.lib()
+        cfg = _n.ServerConfig()
+        L.dlp_server_config_default(ctypes.byref(cfg))
+        cfg.slice_us, cfg.pass_budget = slice_us, pass_budget
+        cfg.memory_budget_bytes, cfg.max_batches_per_step, cfg.serial = memory_budget_bytes, max_batches_per_step, \
+            int(bool(serial))
+        self.engine = engine
+        self._h = ctypes.c_void_p()
+        _n.check(L.dlp_server_create(engine._h, ctypes.byref(cfg), ctypes.byref(self._h)))
+
+    def submit(self, gid: int, batch_index: int, batch: Batch) -> int:
+        req = _n.Request(gid, batch_index, batch.view(), 0.0)
+        rid = ctypes.c_int(-1)
+        _n.check(_n.lib().dlp_server_submit(self._h, ctypes.byref(req), ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self) -> list[int]:
+        ids = (ctypes.c_int * 4096)()
+        nc = ctypes.c_int(0)
+        _n.check(_n.lib().dlp_server_poll(self._h, ids, 4096, ctypes.byref(nc)))
+        return [ids[i] for i in range(min(nc.value, 4096))]
+
+    @property
+    def pending(self) -> int:
+        return int(_n.lib().dlp_server_pending(self._h))
+
+    def drain(self) -> list[int]:
+        done = []
+        while self.pending:
+            done += self.poll()
+        return done
+
+    def result(self, rid: int) -> dict:
+        r = _n.RequestResult()
+        _n.check(_n.lib().dlp_server_result(self._h, rid, ctypes.byref(r)))
+        return _result_dict(r)
+
+    def replay(self, trace: list[tuple[float, int, int, Batch]]) -> tuple[list[dict], float]:
+        """trace: (arrival seconds, graph id, batch index, Batch), sorted by
+        arrival. Returns per-request results and the makespan in seconds."""
+        n = len(trace)
+        reqs = (_n.Request * max(n, 1))()
+        for i, (t, g, b, bt) in enumerate(trace):
+            reqs[i] = _n.Request(g, b, bt.view(), t)
+        out = (_n.RequestResult * max(n, 1))()
+        span = ctypes.c_double(0.0)
+        _n.check(_n.lib().dlp_server_replay(self._h, n, reqs, out, ctypes.byref(span)))
+        return [_result_dict(out[i]) for i in range(n)], float(span.value)
+
+    def close(self) -> None:
+        if self._h:
+            _n.lib().dlp_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _result_dict(r) -> dict:
+    return {"graph_id": r.graph_id, "batch_index": r.batch_index, "status": r.status, "arrival_s": r.arrival_s,
+            "admit_s": r.admit_s, "finish_s": r.finish_s, "steps": r.steps, "stats": r.stats.as_dict()}
 
 
 class DeviceArray:

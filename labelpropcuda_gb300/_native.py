@@ -52,6 +52,29 @@ class BatchStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("slice_us", ctypes.c_double), ("pass_budget", ctypes.c_int),
+        ("memory_budget_bytes", ctypes.c_size_t), ("max_batches_per_step", ctypes.c_int),
+        ("serial", ctypes.c_int),
+    ]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [
+        ("graph_id", ctypes.c_int), ("batch_index", ctypes.c_int), ("batch", BatchView),
+        ("arrival_s", ctypes.c_double),
+    ]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [
+        ("graph_id", ctypes.c_int), ("batch_index", ctypes.c_int), ("status", ctypes.c_int),
+        ("arrival_s", ctypes.c_double), ("admit_s", ctypes.c_double), ("finish_s", ctypes.c_double),
+        ("steps", ctypes.c_int), ("stats", BatchStats),
+    ]
+
+
 # status codes
 DLP_OK = 0
 DLP_ERR_INVALID_ARGUMENT = 1
@@ -126,6 +149,20 @@ _SIGNATURES = {
     "dlp_engine_elapsed_ms": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "dlp_engine_read_labels": (_I, [_P, _I, _P]),
     "dlp_engine_artefact": (_I, [_P, _I, _I, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
+    "dlp_engine_step_sliced": (_I, [_P, _I, _P, _P, ctypes.POINTER(BatchView), _I, ctypes.c_double, c_int_p, c_int_p,
+                                    c_int_p]),
+    "dlp_engine_graph_nodes": (_I, [_P, _I]),
+    "dlp_engine_in_progress": (_I, [_P, _I]),
+    "dlp_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
+    "dlp_server_create": (_I, [_P, ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
+    "dlp_server_destroy": (_I, [_P]),
+    "dlp_server_clock": (ctypes.c_double, [_P]),
+    "dlp_server_submit": (_I, [_P, ctypes.POINTER(Request), c_int_p]),
+    "dlp_server_poll": (_I, [_P, c_int_p, _I, c_int_p]),
+    "dlp_server_result": (_I, [_P, _I, ctypes.POINTER(RequestResult)]),
+    "dlp_server_pending": (_I, [_P]),
+    "dlp_server_replay": (_I, [_P, _I, ctypes.POINTER(Request), ctypes.POINTER(RequestResult),
+                               ctypes.POINTER(ctypes.c_double)]),
     "dlp_mark_deletions": (_I, [_P, _P, _P, _P, _P, _I, _I, _P]),
     "dlp_build_sparsified_subgraph": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _I, _P, ctypes.c_float,
                                            _P, _P, _P, c_int_p, c_int_p, _P]),

@@ -95,7 +95,9 @@ struct GraphSlot {
   int seq = 0;
   int prev_d = 0;
   int last_inserted = 0;
-  int last_bc = -1;  // bc slot of the graph in the last step it took part in
+  // a batch whose propagation continues in a later sliced step
+  bool inflight = false;
+  GraphRec inflight_rec{};
   std::vector<int> seq_batch;
   std::vector<int> seq_step;  // engine step of each application
 
@@ -139,7 +141,10 @@ struct dlp_engine {
   int steps = 0;
   cudaEvent_t ev[kStepRing][2];
   bool ev_made = false;
-  std::vector<int> step_graphs;  // graphs of the last step, in bc-slot order
+  int2 *progress_dev = nullptr;     // per launch position: {finished, passes}
+  int2 *progress_host = nullptr;    // pinned copy
+  int inflight = 0;                 // graphs whose batch continues in a later step
+  std::vector<int> last_finished;   // graphs whose batch ended in the last sliced step
 
   ~dlp_engine() {
     cudaSetDevice(device);
@@ -150,6 +155,7 @@ struct dlp_engine {
         delete g;
       }
     for (void *p : owned) cudaFree(p);
+    if (progress_host) cudaFreeHost(progress_host);
     for (int i = 0; i < 2; ++i) {
       if (recs_host[i]) cudaFreeHost(recs_host[i]);
       if (pinned[i]) cudaFreeHost(pinned[i]);
@@ -239,7 +245,11 @@ int reset_graph(dlp_engine *e, GraphSlot *g, int gid) {
   g->seq = 0;
   g->prev_d = 0;
   g->last_inserted = 0;
-  g->last_bc = -1;
+  if (g->inflight) {
+    g->inflight = false;
+    --e->inflight;
+  }
+  DLP_CUDA_TRY(cudaMemset(e->bc_all + gid, 0, sizeof(BatchCounters)));
   g->seq_batch.clear();
   g->seq_step.clear();
   return DLP_OK;
@@ -274,14 +284,32 @@ int device_error(dlp_engine *e) {
   return DLP_OK;
 }
 
-// One launch over `count` graphs with device-resident batch views.
-int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx, const dlp_batch_view *dv) {
-  if (count <= 0) return DLP_OK;
-  if (count > e->max_graphs || count > dlp::engine::kMaxGraphs)
+// Options of a sliced launch (continuous batching); the default runs every
+// batch of the launch to its end.
+struct SliceOpts {
+  int pass_budget = 0;
+  unsigned long long slice_ns = 0;
+  bool resume = false;  // also continue every graph whose batch is unfinished
+};
+
+// One launch over `count` graphs that start a batch (device-resident batch
+// views), followed, when opts.resume, by every graph whose batch continues.
+int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx, const dlp_batch_view *dv,
+                const SliceOpts &opts = SliceOpts()) {
+  std::vector<int> resumed;
+  if (opts.resume)
+    for (int gid = 0; gid < static_cast<int>(e->graphs.size()); ++gid)
+      if (e->graphs[gid] && e->graphs[gid]->inflight) resumed.push_back(gid);
+  const int total = count + static_cast<int>(resumed.size());
+  if (total <= 0) return DLP_OK;
+  if (total > e->max_graphs || total > dlp::engine::kMaxGraphs)
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "too many graphs in one step");
   for (int i = 0; i < count; ++i) {
     GraphSlot *g = slot_of(e, gids[i]);
     if (!g) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph id");
+    if (g->inflight)
+      return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "graph " + std::to_string(gids[i]) +
+                                                     " has a batch in progress (continue it with a sliced step)");
     for (int j = 0; j < i; ++j)
       if (gids[j] == gids[i]) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "a graph appears twice in one step");
     DLP_TRY(check_view(&dv[i], g->n));
@@ -301,7 +329,7 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
     d.sub_local = g->sub_local;
     d.del_pre = g->del_pre;
     d.del_keep = g->del_keep;
-    d.bc = e->bc_all + i;
+    d.bc = e->bc_all + gids[i];
     d.stats_slot = g->stats + (g->seq % kStepRing);
     BatchArgs a{};
     a.batch = batch_idx[i];
@@ -325,25 +353,34 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
     a.spec = e->cfg.semantics == DLP_SEMANTICS_SPEC;
     a.record = e->cfg.record != 0;
     a.solo = e->cfg.small_frontier_solo != 0;
+    a.pass0 = 0;
     a.timeout_ns = static_cast<unsigned long long>(to * 1e9);
     rh[i].st = d;
     rh[i].ba = a;
   }
-  DLP_CUDA_TRY(cudaMemcpyAsync(e->recs_dev + (p ? e->max_graphs : 0), rh, sizeof(GraphRec) * count,
-                               cudaMemcpyHostToDevice, e->stream));
+  for (size_t j = 0; j < resumed.size(); ++j) rh[count + j] = e->graphs[resumed[j]]->inflight_rec;
+  GraphRec *recs = e->recs_dev + (p ? e->max_graphs : 0);
+  DLP_CUDA_TRY(cudaMemcpyAsync(recs, rh, sizeof(GraphRec) * total, cudaMemcpyHostToDevice, e->stream));
   DLP_CUDA_TRY(cudaEventRecord(e->recs_free[p], e->stream));
-  DLP_CUDA_TRY(cudaMemsetAsync(e->bc_all, 0, sizeof(BatchCounters) * count, e->stream));
+  dlp::engine::launch_zero_counters(recs, count, e->stream);
+  DLP_CUDA_TRY(cudaGetLastError());
+  // every step_sliced call reads back which batches ended, budget or not
+  const bool sliced = opts.resume || opts.pass_budget > 0 || opts.slice_ns > 0;
   EngineArgs args{};
-  args.recs = e->recs_dev + (p ? e->max_graphs : 0);
-  args.ng = count;
+  args.recs = recs;
+  args.ng = total;
+  args.ng_new = count;
   args.ectl = e->ectl;
   args.timeout_ns = static_cast<unsigned long long>(to * 1e9);
   args.solo = e->cfg.small_frontier_solo < 0 ? 3 : e->cfg.small_frontier_solo;
+  args.pass_budget = opts.pass_budget;
+  args.slice_ns = opts.slice_ns;
+  args.tag = e->steps + 1;
+  args.progress = sliced ? e->progress_dev : nullptr;
   DLP_CUDA_TRY(cudaEventRecord(e->ev[slot][0], e->stream));
   void *kargs[] = {&args};
   DLP_TRY(dlp::launch_cooperative(e->kernel, e->grid, dlp::session::kBlock, kargs, e->smem, e->stream));
   DLP_CUDA_TRY(cudaEventRecord(e->ev[slot][1], e->stream));
-  e->step_graphs.assign(gids, gids + count);
   for (int i = 0; i < count; ++i) {
     GraphSlot *g = e->graphs[gids[i]];
     if (static_cast<int>(g->seq_batch.size()) <= g->seq) {
@@ -354,10 +391,31 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
     g->seq_step[g->seq] = e->steps;
     g->prev_d = dv[i].num_deleted;
     g->last_inserted = dv[i].num_inserted;
-    g->last_bc = i;
     ++g->seq;
   }
   ++e->steps;
+  if (!sliced) return DLP_OK;
+  // which batches ended: the rest continue from their recorded pass
+  DLP_CUDA_TRY(cudaMemcpyAsync(e->progress_host, e->progress_dev, sizeof(int2) * total, cudaMemcpyDeviceToHost,
+                               e->stream));
+  DLP_CUDA_TRY(cudaStreamSynchronize(e->stream));
+  DLP_TRY(device_error(e));
+  e->last_finished.clear();
+  for (int i = 0; i < total; ++i) {
+    const int gid = i < count ? gids[i] : resumed[i - count];
+    GraphSlot *g = e->graphs[gid];
+    const int2 pr = e->progress_host[i];
+    const bool was = g->inflight;
+    if (pr.x) {
+      g->inflight = false;
+      e->last_finished.push_back(gid);
+    } else {
+      g->inflight = true;
+      g->inflight_rec = rh[i];
+      g->inflight_rec.ba.pass0 = pr.y;
+    }
+    e->inflight += static_cast<int>(g->inflight) - static_cast<int>(was);
+  }
   return DLP_OK;
 }
 
@@ -498,10 +556,14 @@ int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_bu
   if ((st = dalloc(&e->ectl, 1, e->owned, e->owned_bytes)) ||
       (st = dalloc(&e->ctl_all, max_graphs, e->owned, e->owned_bytes)) ||
       (st = dalloc(&e->bc_all, max_graphs, e->owned, e->owned_bytes)) ||
-      (st = dalloc(&e->recs_dev, 2 * static_cast<size_t>(max_graphs), e->owned, e->owned_bytes)))
+      (st = dalloc(&e->recs_dev, 2 * static_cast<size_t>(max_graphs), e->owned, e->owned_bytes)) ||
+      (st = dalloc(&e->progress_dev, max_graphs, e->owned, e->owned_bytes)))
     return bail(st);
+  if (cudaMallocHost(&e->progress_host, sizeof(int2) * max_graphs) != cudaSuccess)
+    return bail(dlp::fail(DLP_ERR_OUT_OF_MEMORY, "pinned host allocation failed"));
   if (cudaMemset(e->ectl, 0, sizeof(EngineCtl)) != cudaSuccess ||
-      cudaMemset(e->ctl_all, 0, sizeof(SessionCtl) * max_graphs) != cudaSuccess)
+      cudaMemset(e->ctl_all, 0, sizeof(SessionCtl) * max_graphs) != cudaSuccess ||
+      cudaMemset(e->bc_all, 0, sizeof(BatchCounters) * max_graphs) != cudaSuccess)
     return bail(dlp::fail(DLP_ERR_CUDA, "initialisation failed"));
   e->graphs.assign(max_graphs, nullptr);
   *out = e;
@@ -633,6 +695,7 @@ int dlp_engine_remove_graph(dlp_engine *e, int graph_id) {
   if (!g) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph id");
   DLP_CUDA_TRY(cudaSetDevice(e->device));
   DLP_CUDA_TRY(cudaStreamSynchronize(e->stream));
+  if (g->inflight) --e->inflight;
   e->used -= std::min(e->used, g->bytes);
   g->free_all();
   delete g;
@@ -683,6 +746,38 @@ int dlp_engine_step_device(dlp_engine *e, int count, const int *graph_ids, const
   return launch_step(e, count, graph_ids, batch_indices, device_batches);
 }
 
+int dlp_engine_step_sliced(dlp_engine *e, int count, const int *graph_ids, const int *batch_indices,
+                           const dlp_batch_view *device_batches, int pass_budget, double slice_us,
+                           int *finished_ids, int *num_finished, int *num_continuing) {
+  dlp::clear_error();
+  if (!e || count < 0 || (count > 0 && (!graph_ids || !batch_indices || !device_batches)) || !num_finished)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+  if (pass_budget < 0 || !(slice_us >= 0.0)) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "negative budget");
+  *num_finished = 0;
+  if (num_continuing) *num_continuing = e->inflight;
+  DLP_CUDA_TRY(cudaSetDevice(e->device));
+  SliceOpts o;
+  o.pass_budget = pass_budget;
+  o.slice_ns = static_cast<unsigned long long>(slice_us * 1e3);
+  o.resume = true;
+  e->last_finished.clear();
+  DLP_TRY(launch_step(e, count, graph_ids, batch_indices, device_batches, o));
+  *num_finished = static_cast<int>(e->last_finished.size());
+  if (finished_ids) std::copy(e->last_finished.begin(), e->last_finished.end(), finished_ids);
+  if (num_continuing) *num_continuing = e->inflight;
+  return DLP_OK;
+}
+
+int dlp_engine_graph_nodes(const dlp_engine *e, int graph_id) {
+  GraphSlot *g = slot_of(const_cast<dlp_engine *>(e), graph_id);
+  return g ? g->n : -1;
+}
+
+int dlp_engine_in_progress(const dlp_engine *e, int graph_id) {
+  GraphSlot *g = slot_of(const_cast<dlp_engine *>(e), graph_id);
+  return g && g->inflight ? 1 : 0;
+}
+
 int dlp_engine_synchronize(dlp_engine *e) {
   dlp::clear_error();
   if (!e) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null engine");
@@ -697,6 +792,7 @@ int dlp_engine_stats(dlp_engine *e, int graph_id, int batch_index, dlp_batch_sta
   if (!g || !out) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph or null out");
   const int seq = find_seq(g, batch_index);
   if (seq < 0 || g->seq - seq > kStepRing) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "no statistics kept for that batch");
+  if (g->inflight && seq == g->seq - 1) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "that batch is still in progress");
   DLP_CUDA_TRY(cudaSetDevice(e->device));
   DLP_CUDA_TRY(cudaStreamSynchronize(e->stream));
   DLP_TRY(device_error(e));
@@ -734,7 +830,7 @@ int dlp_engine_debug(dlp_engine *e, int *out4) {
   out4[0] = c.err;
   out4[1] = c.where;
   out4[2] = c.where_pass;
-  out4[3] = c.solo_passes;
+  out4[3] = std::max(c.solo_passes[0], c.solo_passes[1]);
   return DLP_OK;
 }
 
@@ -742,6 +838,7 @@ int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels) {
   dlp::clear_error();
   GraphSlot *g = slot_of(e, graph_id);
   if (!g || !host_labels) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph or null out");
+  if (g->inflight) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "the graph's batch is still in progress");
   DLP_TRY(dlp_engine_synchronize(e));
   int cb = 0;
   DLP_CUDA_TRY(cudaMemcpy(&cb, &e->ctl_all[graph_id].cur_buf, sizeof(int), cudaMemcpyDeviceToHost));
@@ -753,10 +850,11 @@ int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, 
   dlp::clear_error();
   GraphSlot *g = slot_of(e, graph_id);
   if (!g || !count) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph or null count");
+  if (g->inflight) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "the graph's batch is still in progress");
   DLP_TRY(dlp_engine_synchronize(e));
   const DevState &d = g->st;
   BatchCounters bc{};
-  if (g->last_bc >= 0) DLP_CUDA_TRY(cudaMemcpy(&bc, e->bc_all + g->last_bc, sizeof(bc), cudaMemcpyDeviceToHost));
+  if (g->seq > 0) DLP_CUDA_TRY(cudaMemcpy(&bc, e->bc_all + graph_id, sizeof(bc), cudaMemcpyDeviceToHost));
   dlp_batch_stats last{};
   if (g->seq > 0)
     DLP_CUDA_TRY(cudaMemcpy(&last, g->stats + (g->seq - 1) % kStepRing, sizeof(last), cudaMemcpyDeviceToHost));

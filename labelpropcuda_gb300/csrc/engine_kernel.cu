@@ -226,7 +226,7 @@ __device__ __forceinline__ void frontier_append(const GV &w, bool pred, bool fir
 // the previous batch's propagation wrote (both buffers start a batch equal,
 // src/dynLP.cu:519 and src/iterativePropagation.cu:268-270).
 __device__ void phase_a(const EngineArgs &e, const Ctx &c, int *pref) {
-  const int ng = e.ng;
+  const int ng = e.ng_new;
   auto prev_touched = [&](int g) {
     const GraphRec &r = e.recs[g];
     return r.ba.seq > 0 ? r.st.ctl->touched_count[(r.ba.seq - 1) & 1] : 0;
@@ -289,7 +289,7 @@ __device__ void phase_a(const EngineArgs &e, const Ctx &c, int *pref) {
 // Host-status update (ref: delete, insert, then ground truth,
 // src/dynLP.cu:117-130; spec: deletions win) and dirty-row marking.
 __device__ void phase_b(const EngineArgs &e, const Ctx &c, int *pref) {
-  const int ng = e.ng;
+  const int ng = e.ng_new;
   int total = flat_build(pref, ng, [&](int g) {
     const BatchArgs &a = e.recs[g].ba;
     return a.D + a.I + a.G;
@@ -356,7 +356,7 @@ __device__ void phase_b(const EngineArgs &e, const Ctx &c, int *pref) {
 // ---------------------------------------------------------------- phase C ---
 // Live-row compaction, deletion marks and the tau filter.
 __device__ void phase_c(const EngineArgs &e, const Ctx &c, int *pref) {
-  const int ng = e.ng;
+  const int ng = e.ng_new;
   int total = flat_build(pref, ng, [&](int g) { return e.recs[g].st.bc->num_dirty; });
   flat_groups(c, pref, ng, total, [&](int g, int item, bool valid, int gl, int grp) {
     const GV w = view(e, g);
@@ -511,7 +511,7 @@ __device__ void phase_c(const EngineArgs &e, const Ctx &c, int *pref) {
 
 // ---------------------------------------------------------------- phase D ---
 __device__ void phase_d_frontier(const EngineArgs &e, const Ctx &c, int *pref) {
-  const int ng = e.ng;
+  const int ng = e.ng_new;
   const int total = flat_build(pref, ng, [&](int g) { return e.recs[g].st.bc->num_seeds; });
   flat_threads(c, pref, ng, total, [&](int g, int i, bool valid) {
     const GV w = view(e, g);
@@ -543,7 +543,7 @@ __device__ __forceinline__ int hook_count(const GV &w) {
 // then pointer jumping to the root (:108-121), until a hook pass of that
 // graph changes nothing. -1 stands for a vertex that is not new this batch.
 __device__ bool phase_d_sv(const EngineArgs &e, const Ctx &c, int *pref) {
-  const int ng = e.ng;
+  const int ng = e.ng_new;
   for (int r = 0; r < kMaxHookRounds; ++r) {
     auto active = [&](int g) {
       const BatchCounters *bc = e.recs[g].st.bc;
@@ -594,7 +594,7 @@ __device__ bool phase_d_sv(const EngineArgs &e, const Ctx &c, int *pref) {
 // Component count and fixed-point supernode weights per component root
 // (src/labelInitialization.cu:59-88).
 __device__ void phase_e(const EngineArgs &e, const Ctx &c, int *pref) {
-  const int ng = e.ng;
+  const int ng = e.ng_new;
   auto count = [&](int g) {
     const GV w = view(e, g);
     return w.comp_path() ? w.a.I : 0;
@@ -653,7 +653,7 @@ __device__ void phase_e(const EngineArgs &e, const Ctx &c, int *pref) {
 
 // ---------------------------------------------------------------- phase F ---
 __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
-  const int ng = e.ng;
+  const int ng = e.ng_new;
   const int total = flat_build(pref, ng, [&](int g) { return e.recs[g].ba.I; });
   for (int item = c.gtid; item < total; item += c.nthreads) {
     const int g = locate(pref, ng, item);
@@ -812,13 +812,26 @@ __device__ __forceinline__ void wide_row(const DevState &s, const float *src, fl
   }
 }
 
-// A graph takes part in pass k while its frontier is not empty and k is below
-// its max_iter; passes counts the passes it ran.
+// A graph takes part in the launch's pass k (its own pass k + pass0) while its
+// frontier is not empty and its pass is below max_iter; passes counts the
+// passes it ran.
 __device__ __forceinline__ bool graph_in_pass(const GraphRec &r, int k, int &nn, int &nw) {
   const BatchCounters *bc = r.st.bc;
-  nn = ld_relaxed_i32(&bc->front_count[k % 3][0]);
-  nw = ld_relaxed_i32(&bc->front_count[k % 3][1]);
-  return nn + nw > 0 && k < r.ba.max_iter;
+  const int kg = k + r.ba.pass0;
+  nn = ld_relaxed_i32(&bc->front_count[kg % 3][0]);
+  nw = ld_relaxed_i32(&bc->front_count[kg % 3][1]);
+  return nn + nw > 0 && kg < r.ba.max_iter;
+}
+
+// True once the launch's time slice has run out (checked by thread 0 of block
+// 0 only, which recorded the launch's start).
+__device__ __forceinline__ bool slice_over(const EngineArgs &e) {
+  return e.slice_ns != 0 && global_timer_ns() - e.ectl->t_launch > e.slice_ns;
+}
+
+// A stop request for pass k of this launch (EngineCtl::sub_stop, slice_stop).
+__device__ __forceinline__ unsigned long long stop_code(const EngineArgs &e, int k) {
+  return (static_cast<unsigned long long>(static_cast<unsigned>(e.tag)) << 32) | static_cast<unsigned>(k);
 }
 
 // Solo mode: when all graphs' frontiers together are small, block 0 runs the
@@ -851,7 +864,7 @@ struct SoloCache {
   unsigned short graph[kVT];
   unsigned char len[kVT];        // live row length, kWideLen when longer than 32
   signed char gt[kVT];
-  unsigned char flags[kVT];      // bit0 written, bit1 in a frontier, bit2 graph's cur_buf
+  unsigned char flags[kVT];      // bit0 written, bit1 in a frontier, bit2 buffer read at stint pass 0
   int lastpass[kMaxGraphs];      // last pass each graph took part in during the stint
   int cnt[2];
   int used;
@@ -883,7 +896,7 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
       const int len = s.act_len[v];
       c.len[h] = len > kNarrowMax ? kWideLen : static_cast<unsigned char>(len);
       c.graph[h] = static_cast<unsigned short>(g);
-      c.flags[h] = static_cast<unsigned char>((s.ctl->cur_buf & 1) << 2);
+      c.flags[h] = static_cast<unsigned char>(((s.ctl->cur_buf ^ e.recs[g].ba.pass0) & 1) << 2);
       c.row[h] = -1;
       c.mark[h] = -1;
       atomicAdd(&c.used, 1);
@@ -896,7 +909,7 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
 }
 
 template <int G>
-__device__ void solo_passes(const EngineArgs &e, int k0, SoloCache &c) {
+__device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c) {
   const int ng = e.ng;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int kWarps = kBlock / 32;
@@ -912,13 +925,13 @@ __device__ void solo_passes(const EngineArgs &e, int k0, SoloCache &c) {
   }
   __syncthreads();
   int max_iter = 0x7fffffff;
-  for (int g = 0; g < ng; ++g) max_iter = min(max_iter, e.recs[g].ba.max_iter);
+  for (int g = 0; g < ng; ++g) max_iter = min(max_iter, e.recs[g].ba.max_iter - e.recs[g].ba.pass0);
   // F_k0 of every graph into the table and list 0
   for (int g = warp; g < ng; g += kWarps) {
     const GraphRec &r = e.recs[g];
     int nn, nw;
     if (!graph_in_pass(r, k0, nn, nw)) continue;
-    const int *gl_list = r.st.flist + static_cast<size_t>(k0 % 3) * r.st.n;
+    const int *gl_list = r.st.flist + static_cast<size_t>((k0 + r.ba.pass0) % 3) * r.st.n;
     for (int i = lane; i < nn + nw; i += 32) {
       const int v = i < nn ? gl_list[i] : gl_list[r.st.n - 1 - (i - nn)];
       const int slot = vt_slot(c, e, g, v);
@@ -951,7 +964,8 @@ __device__ void solo_passes(const EngineArgs &e, int k0, SoloCache &c) {
     if (tid == 0) c.cnt[p ^ 1] = 0;
     for (int g = tid; g < ng; g += kBlock) {  // the pass's recorded size is counted up below
       const GraphRec &r = e.recs[g];
-      if (r.ba.record && k < kRecordIters) r.st.rec_fsizes[k] = 0;
+      const int kg = k + r.ba.pass0;
+      if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
     }
     __syncthreads();
     if (tid == 0) {
@@ -959,6 +973,11 @@ __device__ void solo_passes(const EngineArgs &e, int k0, SoloCache &c) {
       if (cnt == 0 || cnt > kSoloList || k >= max_iter || c.wide) stop = 1;
       if (c.used + c.need > kVTUse || c.rp_top + c.need > kRP) stop = 1;
       if (((k - k0) & 63) == 63 && global_timer_ns() - t0 > kSoloBudgetNs) stop = 1;
+      if (e.pass_budget > 0 && k >= e.pass_budget) stop = 1;
+      if (((k - k0) & 15) == 15 && slice_over(e)) {
+        stop = 1;
+        e.ectl->slice_stop = stop_code(e, k);  // the grid resumes at pass k and stops there
+      }
       c.stop = stop;
     }
     __syncthreads();
@@ -1040,8 +1059,9 @@ __device__ void solo_passes(const EngineArgs &e, int k0, SoloCache &c) {
         changed = fabsf(nl - old) > r.ba.delta;
         atomicAdd(&r.st.bc->aff_edges, static_cast<unsigned long long>(len));
         atomicAdd(&r.st.bc->front_visits, 1ull);
-        c.lastpass[g] = k;
-        if (r.ba.record && k < kRecordIters) atomicAdd(&r.st.rec_fsizes[k], 1);
+        const int kg = k + r.ba.pass0;
+        c.lastpass[g] = kg;
+        if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
       }
       changed = __shfl_sync(0xffffffffu, changed, 0, G);
       // changed vertex: non-deleted, non-GT neighbours and itself
@@ -1063,22 +1083,26 @@ __device__ void solo_passes(const EngineArgs &e, int k0, SoloCache &c) {
     s.lab0[v] = c.lab[0][i];
     s.lab1[v] = c.lab[1][i];
   }
-  // per-graph pass counts, and the frontier back into set k%3 (set (k+1)%3 empty)
+  // per-graph pass counts, and the frontier back into the set of the graph's
+  // pass k + pass0 (the set after it empty)
   for (int g = tid; g < ng; g += kBlock) {
     BatchCounters *bc = e.recs[g].st.bc;
+    const int kg = k + e.recs[g].ba.pass0;
     if (c.lastpass[g] >= 0) bc->passes = c.lastpass[g] + 1;
-    bc->front_count[k % 3][0] = bc->front_count[k % 3][1] = 0;
-    bc->front_count[(k + 1) % 3][0] = bc->front_count[(k + 1) % 3][1] = 0;
+    bc->front_count[kg % 3][0] = bc->front_count[kg % 3][1] = 0;
+    bc->front_count[(kg + 1) % 3][0] = bc->front_count[(kg + 1) % 3][1] = 0;
   }
   __syncthreads();
   const int cnt = c.cnt[p];
   for (int i = tid; i < cnt; i += kBlock) {
     const int su = c.list[p][i];
-    const DevState &s = e.recs[c.graph[su]].st;
+    const GraphRec &r = e.recs[c.graph[su]];
+    const DevState &s = r.st;
     const int v = static_cast<int>(c.key[su] & 0xffffffffu);
-    int *list = s.flist + static_cast<size_t>(k % 3) * s.n;
-    if (c.len[su] == kWideLen) list[s.n - 1 - atomicAdd(&s.bc->front_count[k % 3][1], 1)] = v;
-    else list[atomicAdd(&s.bc->front_count[k % 3][0], 1)] = v;
+    const int set = (k + r.ba.pass0) % 3;
+    int *list = s.flist + static_cast<size_t>(set) * s.n;
+    if (c.len[su] == kWideLen) list[s.n - 1 - atomicAdd(&s.bc->front_count[set][1], 1)] = v;
+    else list[atomicAdd(&s.bc->front_count[set][0], 1)] = v;
   }
   // vertices that were in a frontier join the touched list the first time in
   // this batch; their stamp is the graph's own last pass (below the next grid
@@ -1096,8 +1120,8 @@ __device__ void solo_passes(const EngineArgs &e, int k0, SoloCache &c) {
     }
   }
   if (tid == 0) {
-    e.ectl->solo_k = k;
-    e.ectl->solo_passes = k - k0;
+    e.ectl->solo_k[slot] = k;
+    e.ectl->solo_passes[slot] = k - k0;
   }
 }
 
@@ -1112,16 +1136,16 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
   // per graph: the set filled two passes from now was last read one pass ago
   for (int g = t0; g < ng; g += nthreads) {
     const GraphRec &r = e.recs[g];
+    const int kg = k + r.ba.pass0;
     int nn, nw;
     const bool in = graph_in_pass(r, k, nn, nw);
-    r.st.bc->front_count[(k + 2) % 3][0] = 0;
-    r.st.bc->front_count[(k + 2) % 3][1] = 0;
+    r.st.bc->front_count[(kg + 2) % 3][0] = 0;
+    r.st.bc->front_count[(kg + 2) % 3][1] = 0;
     if (in) {
-      r.st.bc->passes = k + 1;
-      if (r.ba.record && k < kRecordIters) r.st.rec_fsizes[k] = nn + nw;
+      r.st.bc->passes = kg + 1;
+      if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = nn + nw;
     }
   }
-  const int nset = (k + 1) % 3;
   // rows of at most 32 entries: groups of G lanes
   for (int base = warp0 * GPW; base < tn; base += nwarps * GPW) {
     const int item = base + grp;
@@ -1129,11 +1153,13 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     const int g = valid ? locate(pref, ng, item) : 0;
     const GV w = view(e, g);
     const DevState &s = w.s;
+    const int kg = k + w.a.pass0;
+    const int nset = (kg + 1) % 3;
     const int cb = s.ctl->cur_buf;
-    const float *src = ((cb ^ k) & 1) ? s.lab1 : s.lab0;
-    float *dst = ((cb ^ k) & 1) ? s.lab0 : s.lab1;
-    const unsigned stamp = w.g0 + static_cast<unsigned>(k) + 1u;
-    const int u = valid ? s.flist[static_cast<size_t>(k % 3) * s.n + (item - pref[g])] : 0;
+    const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
+    float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
+    const unsigned stamp = w.g0 + static_cast<unsigned>(kg) + 1u;
+    const int u = valid ? s.flist[static_cast<size_t>(kg % 3) * s.n + (item - pref[g])] : 0;
     auto mark = [&](bool cand, int v) {
       bool fresh = false, first = false;
       if (cand) {
@@ -1153,11 +1179,13 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     const int g = locate(pref2, ng, wi);
     const GV w = view(e, g);
     const DevState &s = w.s;
+    const int kg = k + w.a.pass0;
+    const int nset = (kg + 1) % 3;
     const int cb = s.ctl->cur_buf;
-    const float *src = ((cb ^ k) & 1) ? s.lab1 : s.lab0;
-    float *dst = ((cb ^ k) & 1) ? s.lab0 : s.lab1;
-    const unsigned stamp = w.g0 + static_cast<unsigned>(k) + 1u;
-    const int u = s.flist[static_cast<size_t>(k % 3) * s.n + (s.n - 1 - (wi - pref2[g]))];
+    const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
+    float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
+    const unsigned stamp = w.g0 + static_cast<unsigned>(kg) + 1u;
+    const int u = s.flist[static_cast<size_t>(kg % 3) * s.n + (s.n - 1 - (wi - pref2[g]))];
     auto mark = [&](bool cand, int v) {
       bool fresh = false, first = false;
       if (cand) {
@@ -1195,7 +1223,7 @@ constexpr int kSubEntry = 2048;   // enter when the total frontier is at most th
 constexpr int kSubLive = 4096;    // leave when it grows above this
 
 template <int G>
-__device__ bool sub_passes(const EngineArgs &e, int k0, int *pref, int *pref2) {
+__device__ bool sub_passes(const EngineArgs &e, int k0, int slot, int *pref, int *pref2) {
   const int lane = threadIdx.x & 31;
   const int warp0 = blockIdx.x * (kBlock / 32), nwarps = kSubBlocks * (kBlock / 32);
   const int t0 = blockIdx.x * kBlock + threadIdx.x, nthreads = kSubBlocks * kBlock;
@@ -1204,49 +1232,67 @@ __device__ bool sub_passes(const EngineArgs &e, int k0, int *pref, int *pref2) {
   for (;; ++k) {
     int tn, tw;
     pass_sizes(e, k, pref, pref2, tn, tw);
-    // a stop request is tagged with this stint's first pass, so one left over
-    // from an earlier stint is never taken for this one
-    const bool stop = ld_relaxed_i32(&e.ectl->sub_stop) == k0 + 1;
-    if (tn + tw == 0 || tn + tw > kSubLive || stop) break;
+    const bool stop = ld_relaxed_u64(&e.ectl->sub_stop) == stop_code(e, k);
+    if (tn + tw == 0 || tn + tw > kSubLive || stop || (e.pass_budget > 0 && k >= e.pass_budget)) break;
     run_pass<G>(e, k, pref, tn, pref2, tw, lane, warp0 + (threadIdx.x >> 5), nwarps, t0, nthreads);
-    if (t0 == 0 && ((k - k0) & 31) == 31 && global_timer_ns() - start > 100000000ull) e.ectl->sub_stop = k0 + 1;
+    if (t0 == 0 && ((k - k0) & 31) == 31 && global_timer_ns() - start > 100000000ull)
+      e.ectl->sub_stop = stop_code(e, k + 1);
+    if (t0 == 0 && ((k - k0) & 7) == 7 && slice_over(e)) {
+      e.ectl->sub_stop = stop_code(e, k + 1);
+      e.ectl->slice_stop = stop_code(e, k + 1);
+    }
     if (!grid_sync_n(&e.ectl->sub_bar, kSubBlocks, &e.ectl->err, e.timeout_ns)) return false;
   }
   if (t0 == 0) {
-    e.ectl->solo_k = k;
-    e.ectl->solo_passes = k - k0;
+    e.ectl->solo_k[slot] = k;
+    e.ectl->solo_passes[slot] = k - k0;
   }
   return true;
 }
 
+// The propagation passes of the launch; k_end is the first pass not run (the
+// graphs whose frontier is live at k_end continue in a later launch).
 template <int G>
-__device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2, SoloCache &solo) {
+__device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2, SoloCache &solo, int &k_end) {
   int no_small_at = -1;  // a pass the small modes declined goes to the full grid
-  for (int k = 0;; ++k) {
+  int stint = 0;
+  int k = 0;
+  for (;; ++k) {
     int tn, tw;
     pass_sizes(e, k, pref, pref2, tn, tw);
     if (tn + tw == 0) break;
+    if (e.pass_budget > 0 && k >= e.pass_budget) break;
+    if (ld_relaxed_u64(&e.ectl->slice_stop) == stop_code(e, k)) break;
     if (c.gtid == 0) e.ectl->where_pass = k;
     const bool solo_ok = (e.solo & 1) && tn + tw <= kSoloEntry && k != no_small_at;
     const bool sub_ok = !solo_ok && (e.solo & 2) && gridDim.x > 2 * kSubBlocks && tn + tw <= kSubEntry &&
                         k != no_small_at;
     if (solo_ok || sub_ok) {
       if (solo_ok) {
-        if (blockIdx.x == 0) solo_passes<G>(e, k, solo);
+        if (blockIdx.x == 0) solo_passes<G>(e, k, stint & 1, solo);
       } else if (blockIdx.x < kSubBlocks) {
-        if (!sub_passes<G>(e, k, pref, pref2)) return false;
+        if (!sub_passes<G>(e, k, stint & 1, pref, pref2)) return false;
       }
       if (!grid_sync(&e.ectl->bar, &e.ectl->err, e.timeout_ns)) return false;
-      const int done = ld_relaxed_i32(&e.ectl->solo_passes);
-      const int kk = ld_relaxed_i32(&e.ectl->solo_k);
+      const int done = ld_relaxed_i32(&e.ectl->solo_passes[stint & 1]);
+      const int kk = ld_relaxed_i32(&e.ectl->solo_k[stint & 1]);
+      ++stint;
       if (done == 0) no_small_at = k;
       k = kk - 1;  // the loop increment resumes at pass kk
       continue;
     }
     run_pass<G>(e, k, pref, tn, pref2, tw, c.lane, c.gwarp, c.nwarps, c.gtid, c.nthreads);
+    if (c.gtid == 0 && slice_over(e)) e.ectl->slice_stop = stop_code(e, k + 1);
     if (!grid_sync(&e.ectl->bar, &e.ectl->err, e.timeout_ns)) return false;
   }
+  k_end = k;
   return true;
+}
+
+// A graph's batch ends in this launch when it takes no part in pass k_end.
+__device__ __forceinline__ bool batch_done(const GraphRec &r, int k_end) {
+  int nn, nw;
+  return !graph_in_pass(r, k_end, nn, nw);
 }
 
 // ---------------------------------------------------------------- phase H ---
@@ -1254,10 +1300,11 @@ __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2
 // (src/iterativePropagation.cu:224-235; earlier ground truth already is), and
 // the accuracy counters (src/dynLP.cu:65-85) updated at every vertex whose
 // status or label may have changed.
-__device__ void phase_h(const EngineArgs &e, const Ctx &c, int *pref) {
+__device__ void phase_h(const EngineArgs &e, const Ctx &c, int *pref, int k_end) {
   const int ng = e.ng;
   const int total = flat_build(pref, ng, [&](int g) {
     const GraphRec &r = e.recs[g];
+    if (!batch_done(r, k_end)) return 0;
     return r.ba.G + r.ba.D + r.st.ctl->touched_count[r.ba.seq & 1] + r.ba.I + r.ba.D + r.ba.G;
   });
   flat_threads(c, pref, ng, total, [&](int g, int i, bool valid) {
@@ -1326,30 +1373,34 @@ __global__ void __launch_bounds__(kBlock, 2) engine_kernel(EngineArgs e) {
   auto at = [&](int phase) {
     if (blockIdx.x == 0 && threadIdx.x == 0) e.ectl->where = phase;
   };
-  at(1);
-  phase_a(e, c, pref);
-  if (!grid_sync(bar, err, to)) return;
-  at(2);
-  phase_b(e, c, pref);
-  if (!grid_sync(bar, err, to)) return;
-  at(3);
-  phase_c(e, c, pref);
-  if (!grid_sync(bar, err, to)) return;
-  at(4);
-  phase_d_frontier(e, c, pref);
-  if (!phase_d_sv(e, c, pref)) return;
-  at(5);
-  if (!grid_sync(bar, err, to)) return;
-  at(6);
-  phase_e(e, c, pref);
-  if (!grid_sync(bar, err, to)) return;
-  at(7);
-  phase_f(e, c, pref);
-  if (!grid_sync(bar, err, to)) return;
+  if (c.gtid == 0) e.ectl->t_launch = global_timer_ns();
+  if (e.ng_new > 0) {  // a launch that only continues batches starts at phase G
+    at(1);
+    phase_a(e, c, pref);
+    if (!grid_sync(bar, err, to)) return;
+    at(2);
+    phase_b(e, c, pref);
+    if (!grid_sync(bar, err, to)) return;
+    at(3);
+    phase_c(e, c, pref);
+    if (!grid_sync(bar, err, to)) return;
+    at(4);
+    phase_d_frontier(e, c, pref);
+    if (!phase_d_sv(e, c, pref)) return;
+    at(5);
+    if (!grid_sync(bar, err, to)) return;
+    at(6);
+    phase_e(e, c, pref);
+    if (!grid_sync(bar, err, to)) return;
+    at(7);
+    phase_f(e, c, pref);
+    if (!grid_sync(bar, err, to)) return;
+  }
   at(8);
-  if (!phase_g<G>(e, c, pref, pref2, solo)) return;
+  int k_end = 0;
+  if (!phase_g<G>(e, c, pref, pref2, solo, k_end)) return;
   at(9);
-  phase_h(e, c, pref);
+  phase_h(e, c, pref, k_end);
   if (!grid_sync(bar, err, to)) return;
   at(10);
 
@@ -1359,6 +1410,11 @@ __global__ void __launch_bounds__(kBlock, 2) engine_kernel(EngineArgs e) {
     const DevState &s = r.st;
     const BatchArgs &a = r.ba;
     const BatchCounters *bc = s.bc;
+    if (!batch_done(r, k_end)) {  // continues in a later launch
+      if (e.progress) e.progress[g] = make_int2(0, k_end + a.pass0);
+      continue;
+    }
+    if (e.progress) e.progress[g] = make_int2(1, bc->passes);
     const GV w = view(e, g);
     const bool comp = w.comp_path();
     const int passes = bc->passes;
@@ -1402,6 +1458,17 @@ template __global__ void engine_kernel<4>(EngineArgs);
 template __global__ void engine_kernel<8>(EngineArgs);
 template __global__ void engine_kernel<16>(EngineArgs);
 template __global__ void engine_kernel<32>(EngineArgs);
+
+// One block per graph that starts a batch: its counters back to zero.
+__global__ void zero_counters_kernel(const GraphRec *recs) {
+  int *p = reinterpret_cast<int *>(recs[blockIdx.x].st.bc);
+  constexpr int kWords = static_cast<int>(sizeof(BatchCounters) / sizeof(int));
+  for (int i = threadIdx.x; i < kWords; i += blockDim.x) p[i] = 0;
+}
+
+void launch_zero_counters(const GraphRec *recs, int ng_new, cudaStream_t stream) {
+  if (ng_new > 0) zero_counters_kernel<<<ng_new, 128, 0, stream>>>(recs);
+}
 
 size_t engine_dynamic_smem() { return sizeof(SoloCache); }
 

@@ -26,7 +26,9 @@ constexpr int kRecordIters = 1 << 17;   // per-pass frontier sizes kept when rec
 constexpr int kNarrowMax = 32;          // rows up to this length use the group path
 constexpr int kRowGroup = 8;            // lanes per row in the bookkeeping phases
 
-// Per-batch counters, zeroed by the host before every launch.
+// Per-batch counters of one graph, zeroed at the start of the launch that
+// begins the graph's batch (they carry over when its propagation is continued
+// by later launches).
 struct BatchCounters {
   int front_count[3][2];  // frontier list sets: [set][0 narrow, 1 wide]
   int num_dirty;
@@ -111,6 +113,7 @@ struct BatchArgs {
   int spec;
   int record;
   int solo;                 // small frontiers run on one block (see phase G)
+  int pass0;                // propagation passes run by earlier launches (0: batch starts here)
   unsigned long long timeout_ns;
 };
 
