@@ -19,6 +19,18 @@ labels), wall clock with the stream synchronised on both sides.
 Reference arm (--impl reference): the reference's path is CUDA only, so its
 CPU counterpart is the oracle's restatement of it (oracle/, a port), run with
 all host threads on the same workload.
+
+Served vs plain (the `served` object of the same line; --no-served skips it):
+a mixed-graph stream of --served-graphs resident graphs (default 64; the
+multi-instance shape with 512 is --served-graphs 512), sizes log-uniform on
+[1e3, 5e5], degree {3,5,7}, 10 batches each. `batched` runs one engine launch
+per batch index over all graphs; `served_saturated` replays every request
+through the continuous-batching server with all of them queued at t = 0;
+`served_poisson` replays them with Poisson arrivals at half the saturated
+request rate (latency = finish - arrival); `plain` is the server in serial
+mode (one request at a time, run to its end — the plain per-batch path) on a
+bounded sample of whole graphs. All three count the same affected edges per
+request; the served paths include the host-to-device copy of every request.
 """
 from __future__ import annotations
 
@@ -305,7 +317,7 @@ def gpu_arm(args, td, rank, world, local_rank):
     kern_s = sum(s["device_ms"] for s in stats0) / 1e3
     achieved = bytes_step / kern_s / 1e9 if kern_s > 0 else 0.0
     traffic = None
-    tf = ROOT / "profiles" / "traffic_batch_kernel_config2.json"
+    tf = ROOT / "profiles" / "traffic_engine_kernel_config2.json"
     if tf.exists():
         try:
             traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
@@ -313,6 +325,7 @@ def gpu_arm(args, td, rank, world, local_rank):
             traffic = None
     # CPU baseline: the oracle, single thread, bounded sample of the same workload
     cpu_edges, cpu_t, cpu_done = cpu_run(p, 1, args.cpu_budget_s)
+    served = None if args.no_served or world > 1 else served_block(args, local_rank)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
@@ -329,15 +342,148 @@ def gpu_arm(args, td, rank, world, local_rank):
                 "timing": "wall clock, stream synchronised on both sides"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "kernel": "dlp::session::batch_kernel", "peak_source": peak_kind,
+                     "kernel": "dlp::engine::engine_kernel<8>", "peak_source": peak_kind,
                      "algorithmic_bytes_per_step": bytes_step},
         "cpu_baseline": {"value": cpu_edges / cpu_t if cpu_t > 0 else 0.0, "unit": UNIT, "cores": 1, "kind": "port",
                          "sample": f"oracle port, 1 thread, first {cpu_done} of {nb} batches of the same workload"},
         "clocks": clocks,
-        "gpu_launches": args.steps * nb,
+        "gpu_launches": args.steps * nb * 2,
     }
+    if served is not None:
+        line["served"] = served
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ------------------------------------------------------ served vs plain -----
+
+def mix_sizes(count: int, lo: float, hi: float, seed: int):
+    """Graph sizes log-uniform on [lo, hi] (numpy PCG64, fixed seed), average
+    degree {3,5,7}[i mod 3], generator seed i."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    n = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(int)
+    return [(int(n[i]), (3, 5, 7)[i % 3], 10, i) for i in range(count)]
+
+
+def make_problems(specs, threads: int):
+    import concurrent.futures as cf
+    import labelpropcuda_gb300 as dlp
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(lambda s: dlp.Problem(*s), specs))
+
+
+def served_block(args, local_rank) -> dict:
+    """The mixed-graph stream: N resident graphs, every graph's 10 batches.
+    batched = one engine step per batch index over all graphs (one launch per
+    step, per-graph convergence); served = the continuous-batching server
+    replaying the requests (all queued at once = saturation, then Poisson at
+    half that request rate); plain = the same server in serial mode (one
+    request at a time, run to its end), on a bounded sample of the trace."""
+    import numpy as np
+    import labelpropcuda_gb300 as dlp
+    from labelpropcuda_gb300 import PackedBatches
+    t_setup = time.perf_counter()
+    specs = mix_sizes(args.served_graphs, 1e3, 5e5, 1000003)
+    probs = make_problems(specs, min(16, os.cpu_count() or 1))
+    eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=args.served_lanes)
+    gids = [eng.add_problem(p) for p in probs]
+    nb = 10
+    for g, p in zip(gids, probs):  # scratch sized up front: no allocation inside the timed runs
+        eng.reserve(g, max(bt.edge_src.size for bt in p.batches), max(bt.deleted.size for bt in p.batches))
+    packed = [PackedBatches([p.batches[b] for p in probs]) for b in range(nb)]
+    setup_s = time.perf_counter() - t_setup
+    vertices = sum(p.num_nodes for p in probs)
+    edges_full = sum(p.num_edges for p in probs)
+
+    def reset_all():
+        for g in gids:
+            eng.reset_graph(g)
+
+    # batched: one launch per step over every graph
+    def batched_run():
+        reset_all()
+        first = eng.steps
+        for b in range(nb):
+            eng.step_device([(g, b, packed[b].view(i)) for i, g in enumerate(gids)])
+        eng.synchronize()
+        ms = [eng.elapsed_ms(first + b, first + b) for b in range(nb)]
+        ae = sum(eng.stats(g, b)["affected_edges"] for g in gids for b in range(nb))
+        return ms, ae
+    b_ms, b_ae = batched_run()
+    batched = {"value": b_ae / (sum(b_ms) / 1e3), "ms_per_step": sum(b_ms) / nb,
+               "step_ms_p50": percentile(b_ms, 0.5), "step_ms_max": max(b_ms),
+               "affected_edges": b_ae, "launches": 2 * nb,
+               "timing": "CUDA events around each step, batches resident in HBM"}
+
+    reqs = [(0.0, g, b, probs[i].batches[b]) for b in range(nb) for i, g in enumerate(gids)]
+
+    srv = dlp.Server(eng, memory_budget_bytes=150 << 30, slice_us=args.slice_us)
+    for g, p in zip(gids, probs):
+        srv.reserve(g, p.batches)
+
+    def replay(trace):
+        reset_all()
+        res, span = srv.replay(trace)
+        bad = [r for r in res if r["status"] != 0]
+        if bad:
+            raise RuntimeError(f"{len(bad)} requests failed: {bad[0]}")
+        return res, span
+
+    # saturation: everything queued at t = 0
+    res, span = replay(reqs)
+    sat_ae = sum(r["stats"]["affected_edges"] for r in res)
+    sat_rate = len(res) / span
+    svc = [1e3 * (r["finish_s"] - r["admit_s"]) for r in res]
+    served_sat = {"value": sat_ae / span, "makespan_s": span, "requests": len(res),
+                  "requests_per_s": sat_rate, "service_ms_p50": percentile(svc, 0.5),
+                  "service_ms_p99": percentile(svc, 0.99)}
+    # Poisson arrivals at half the saturated request rate (each graph's
+    # batches keep their order: arrival k goes to the next request in the list)
+    rng = np.random.default_rng(7)
+    rate = 0.5 * sat_rate
+    times = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    trace = [(float(t), g, b, bt) for t, (_, g, b, bt) in zip(times, reqs)]
+    res, span = replay(trace)
+    srv.close()
+    lat = [1e3 * (r["finish_s"] - r["arrival_s"]) for r in res]
+    p_ae = sum(r["stats"]["affected_edges"] for r in res)
+    served_poisson = {"offered_requests_per_s": rate, "value": p_ae / span, "makespan_s": span,
+                      "latency_ms_p50": percentile(lat, 0.5), "latency_ms_p99": percentile(lat, 0.99),
+                      "latency_ms_max": max(lat)}
+    # plain: serial, bounded sample — whole graphs (all 10 batches each, in
+    # order) taken in a seeded random order until the time budget is used
+    reset_all()
+    srv = dlp.Server(eng, serial=True)
+    for g, p in zip(gids, probs):
+        srv.reserve(g, p.batches)
+    order = np.random.default_rng(11).permutation(len(gids))
+    graphs_done, pl_ae, pl_t, pl_svc = 0, 0, 0.0, []
+    for i in order:
+        if pl_t >= args.plain_budget_s:
+            break
+        res, span = srv.replay([(0.0, gids[i], b, probs[i].batches[b]) for b in range(nb)])
+        pl_ae += sum(r["stats"]["affected_edges"] for r in res)
+        pl_t += span
+        pl_svc += [1e3 * (r["finish_s"] - r["admit_s"]) for r in res]
+        graphs_done += 1
+    srv.close()
+    plain_v = pl_ae / pl_t if pl_t > 0 else 0.0
+    plain = {"value": plain_v, "requests": graphs_done * nb, "seconds": pl_t,
+             "service_ms_p50": percentile(pl_svc, 0.5), "service_ms_p99": percentile(pl_svc, 0.99),
+             "sample": f"{graphs_done} of {len(gids)} graphs (seeded random order), all {nb} batches each, "
+                       f"one request at a time"}
+    out = {"workload": (f"mixed-graph stream: {len(probs)} graphs, n log-uniform on [1e3, 5e5] (numpy seed "
+                        f"1000003), degree {{3,5,7}}[i mod 3], generator seed i, 10 batches each (90/1/9), "
+                        f"delta 1e-4, maxIter 1e5, ref semantics; {vertices} vertices, {edges_full} directed "
+                        f"edges in all"),
+           "setup_s": setup_s, "batched": batched, "served_saturated": served_sat,
+           "served_poisson": served_poisson, "plain": plain,
+           "served_over_plain": served_sat["value"] / plain_v if plain_v else None,
+           "batched_over_plain": batched["value"] / plain_v if plain_v else None,
+           "slice_us": args.slice_us, "narrow_lanes": args.served_lanes}
+    eng.close()
+    return out
 
 
 def main(argv=None) -> int:
@@ -351,6 +497,11 @@ def main(argv=None) -> int:
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--ref-budget-s", type=float, default=20.0)
+    ap.add_argument("--served-graphs", type=int, default=64)
+    ap.add_argument("--served-lanes", type=int, default=4)
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--slice-us", type=float, default=1000.0)
+    ap.add_argument("--plain-budget-s", type=float, default=20.0)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -257,6 +257,10 @@ int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, 
 int dlp_engine_step_sliced(dlp_engine *e, int count, const int *graph_ids, const int *batch_indices,
                            const dlp_batch_view *device_batches, int pass_budget, double slice_us,
                            int *finished_ids, int *num_finished, int *num_continuing);
+/* Sizes a graph's batch scratch for batches of up to max_edges new edges and
+ * max_deleted deletions, so that later steps allocate nothing (scratch grows
+ * on demand otherwise). */
+int dlp_engine_reserve(dlp_engine *e, int graph_id, int max_edges, int max_deleted);
 /* Vertex count of a resident graph, -1 for an unknown id. */
 int dlp_engine_graph_nodes(const dlp_engine *e, int graph_id);
 /* 1 while graph_id has a batch in progress in sliced steps, else 0. */
@@ -297,6 +301,10 @@ int dlp_server_create(dlp_engine *e, const dlp_server_config *cfg, dlp_server **
 int dlp_server_destroy(dlp_server *s);
 /* Seconds since the server was created (the clock of dlp_request_result). */
 double dlp_server_clock(const dlp_server *s);
+/* Sizes a graph's staging buffers and its engine scratch for requests up to
+ * the given sizes, so that admission allocates nothing. */
+int dlp_server_reserve(dlp_server *s, int graph_id, int max_inserted, int max_gt, int max_deleted,
+                       int max_edges);
 /* Queues a request (its arrays are copied); *request_id identifies it. */
 int dlp_server_submit(dlp_server *s, const dlp_request *req, int *request_id);
 /* One scheduling round: admits queued requests in arrival order (one batch

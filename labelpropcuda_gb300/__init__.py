@@ -298,6 +298,9 @@ class Engine:
                                                  ctypes.byref(nf), ctypes.byref(nc)))
         return [fin[i] for i in range(nf.value)], nc.value
 
+    def reserve(self, gid: int, max_edges: int, max_deleted: int) -> None:
+        _n.check(_n.lib().dlp_engine_reserve(self._h, gid, max_edges, max_deleted))
+
     def in_progress(self, gid: int) -> bool:
         return bool(_n.lib().dlp_engine_in_progress(self._h, gid))
 
@@ -356,6 +359,12 @@ class Server:
         self.engine = engine
         self._h = ctypes.c_void_p()
         _n.check(L.dlp_server_create(engine._h, ctypes.byref(cfg), ctypes.byref(self._h)))
+
+    def reserve(self, gid: int, batches: list[Batch]) -> None:
+        """Sizes the graph's buffers for the largest of the given batches."""
+        m = lambda f: max((f(b) for b in batches), default=0)
+        _n.check(_n.lib().dlp_server_reserve(self._h, gid, m(lambda b: b.inserted.size), m(lambda b: b.gt_ids.size),
+                                             m(lambda b: b.deleted.size), m(lambda b: b.edge_src.size)))
 
     def submit(self, gid: int, batch_index: int, batch: Batch) -> int:
         req = _n.Request(gid, batch_index, batch.view(), 0.0)

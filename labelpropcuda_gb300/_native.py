@@ -152,6 +152,8 @@ _SIGNATURES = {
     "dlp_engine_step_sliced": (_I, [_P, _I, _P, _P, ctypes.POINTER(BatchView), _I, ctypes.c_double, c_int_p, c_int_p,
                                     c_int_p]),
     "dlp_engine_graph_nodes": (_I, [_P, _I]),
+    "dlp_engine_reserve": (_I, [_P, _I, _I, _I]),
+    "dlp_server_reserve": (_I, [_P, _I, _I, _I, _I, _I]),
     "dlp_engine_in_progress": (_I, [_P, _I]),
     "dlp_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
     "dlp_server_create": (_I, [_P, ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),

@@ -768,6 +768,14 @@ int dlp_engine_step_sliced(dlp_engine *e, int count, const int *graph_ids, const
   return DLP_OK;
 }
 
+int dlp_engine_reserve(dlp_engine *e, int graph_id, int max_edges, int max_deleted) {
+  dlp::clear_error();
+  GraphSlot *g = slot_of(e, graph_id);
+  if (!g || max_edges < 0 || max_deleted < 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph or negative size");
+  DLP_CUDA_TRY(cudaSetDevice(e->device));
+  return grow_graph_scratch(e, g, max_edges, max_deleted);
+}
+
 int dlp_engine_graph_nodes(const dlp_engine *e, int graph_id) {
   GraphSlot *g = slot_of(const_cast<dlp_engine *>(e), graph_id);
   return g ? g->n : -1;

@@ -699,17 +699,28 @@ __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
 // ---------------------------------------------------------------- phase G ---
 // One row of at most 32 live entries by a group of G lanes; calls
 // mark(cand, v) for each slot and for u itself, on every lane.
-template <int G, class Mark>
+// cand[] receives what a changed row marks (src/iterativePropagation.cu:200-216):
+// its non-deleted, non-ground-truth neighbours (cand[0..R)) and the vertex
+// itself (cand[R]), -1 where nothing is marked; bit r of wide_bits is set when
+// cand[r]'s live row is longer than 32 entries. Every load that depends only
+// on the row (own label, neighbour labels, classes and row lengths) is issued
+// before the row's sum is formed, so a row costs three dependent memory round
+// trips (list entry, row, neighbours) before its marks.
+template <int G>
 __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, float *dst, float delta, int u,
-                                           bool valid, int gl, int &len_out, Mark mark) {
+                                           bool valid, int gl, int &len_out, int (&cand)[32 / G + 1],
+                                           unsigned &wide_bits) {
   constexpr int R = 32 / G;
   int rs = 0, len = 0;
+  float old = 0.0f;
   if (valid) {
     rs = s.full_row[u];
     len = s.act_len[u];
+    if (gl == 0) old = src[u];
   }
   float sw[R], sl[R];
   int vv[R];
+  unsigned wb = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int ee = gl + G * r;
@@ -718,11 +729,12 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
     vv[r] = -1;
     if (ee < len) {
       const int2 ent = s.act_adj[rs + ee];
-      vv[r] = ent.x;
       if (ent.x >= 0) {
         const float wt = __int_as_float(ent.y);
         sw[r] = wt;                               // 0 + w
         sl[r] = __fmaf_rn(wt, src[ent.x], 0.0f);  // fma(w, F_v, 0)
+        if (s.gt[ent.x] < 0) vv[r] = ent.x;
+        if (s.act_len[ent.x] > kNarrowMax) wb |= 1u << r;
       }
     }
   }
@@ -741,21 +753,74 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
   }
   int changed = 0;
   if (valid && gl == 0) {
-    const float old = src[u];
     const float nl = updated_label(tw, tl, old);
     dst[u] = nl;
     changed = fabsf(nl - old) > delta;
   }
   changed = __shfl_sync(0xffffffffu, changed, 0, G);
   len_out = len;
-  // changed vertex: non-deleted, non-GT neighbours and itself
-  // (src/iterativePropagation.cu:200-216)
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int v = vv[r];
-    mark(changed && v >= 0 && s.gt[v] < 0, v);
+  for (int r = 0; r < R; ++r) cand[r] = changed ? vv[r] : -1;
+  cand[R] = (changed && gl == 0) ? u : -1;
+  if (len > kNarrowMax) wb |= 1u << R;
+  wide_bits = changed ? wb : 0u;
+}
+
+// Marks of one G-lane group (one row, one graph): every stamp atomic is
+// issued before any result is used, then each of the three lists (narrow
+// rows from the front of set `set`, wide rows from its back, the batch's
+// touched list) gets one reservation for the whole group. The marked set is
+// the same as marking one candidate at a time; only the order of the list
+// entries differs, and nothing depends on that order.
+template <int G>
+__device__ __forceinline__ void group_mark(const GV &w, const int (&cand)[32 / G + 1], unsigned wide_bits,
+                                           unsigned stamp, int set, int gl) {
+  constexpr int C = 32 / G + 1;
+  const DevState &s = w.s;
+  unsigned old[C];
+#pragma unroll
+  for (int r = 0; r < C; ++r) old[r] = cand[r] >= 0 ? atomicMax(&s.front_stamp[cand[r]], stamp) : stamp;
+  int nn = 0, nw = 0, nf = 0;
+#pragma unroll
+  for (int r = 0; r < C; ++r) {
+    if (old[r] < stamp) {
+      if ((wide_bits >> r) & 1u) ++nw;
+      else ++nn;
+    }
+    if (old[r] < w.g0) ++nf;
   }
-  mark(changed && gl == 0, u);
+  // counts packed 10 bits each (a group marks at most 64 vertices)
+  const int mine = nn | (nw << 10) | (nf << 20);
+  int incl = mine;
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o, G);
+    if (gl >= o) incl += t;
+  }
+  const int tot = __shfl_sync(0xffffffffu, incl, G - 1, G);
+  int bn = 0, bw = 0, bf = 0;
+  if (gl == G - 1 && tot != 0) {
+    const int tn = tot & 1023, tw = (tot >> 10) & 1023, tf = tot >> 20;
+    if (tn) bn = atomicAdd(&s.bc->front_count[set][0], tn);
+    if (tw) bw = atomicAdd(&s.bc->front_count[set][1], tw);
+    if (tf) bf = atomicAdd(&s.ctl->touched_count[w.a.seq & 1], tf);
+  }
+  bn = __shfl_sync(0xffffffffu, bn, G - 1, G);
+  bw = __shfl_sync(0xffffffffu, bw, G - 1, G);
+  bf = __shfl_sync(0xffffffffu, bf, G - 1, G);
+  if (mine == 0) return;
+  const int excl = incl - mine;
+  int on = bn + (excl & 1023), ow = bw + ((excl >> 10) & 1023), of = bf + (excl >> 20);
+  int *list = s.flist + static_cast<size_t>(set) * s.n;
+  int *touched = s.touched + static_cast<size_t>(w.a.seq & 1) * s.n;
+#pragma unroll
+  for (int r = 0; r < C; ++r) {
+    if (old[r] < stamp) {
+      if ((wide_bits >> r) & 1u) list[s.n - 1 - ow++] = cand[r];
+      else list[on++] = cand[r];
+    }
+    if (old[r] < w.g0) touched[of++] = cand[r];
+  }
 }
 
 // One row of any length by a whole warp: 256 slots held as lane + 32*j.
@@ -850,15 +915,19 @@ constexpr int kVTUse = kVT / 2;
 constexpr int kRP = 4096;          // row-pool entries
 constexpr int kSoloList = 1024;    // frontier capacity (vertex-table slots)
 constexpr int kSoloEntry = 512;    // enter when the total frontier is at most this
+constexpr int kSoloMaxPasses = 65000;  // per stint, so that per-slot visit counts fit 16 bits
 constexpr unsigned long long kSoloBudgetNs = 100000000ull;
 constexpr unsigned long long kEmptyKey = ~0ull;
 constexpr unsigned char kWideLen = 255;
+constexpr unsigned short kNoRow = 0xffff;
+constexpr int kSoloG = 4;          // lanes per row in the one-block passes
 
 struct SoloCache {
   unsigned long long key[kVT];   // (graph << 32) | vertex, kEmptyKey = free
   float lab[2][kVT];             // the graph's physical buffers 0 and 1
   int mark[kVT];                 // last pass (+1) that put the slot in the next frontier
-  int row[kVT];                  // row-pool offset, -1 = not loaded
+  unsigned short row[kVT];       // row-pool offset, kNoRow = not loaded
+  unsigned short visits[kVT];    // passes of the stint that updated the slot
   int2 rp[kRP];                  // {neighbour slot or -1, weight bits}
   unsigned short list[2][kSoloList];
   unsigned short graph[kVT];
@@ -866,12 +935,16 @@ struct SoloCache {
   signed char gt[kVT];
   unsigned char flags[kVT];      // bit0 written, bit1 in a frontier, bit2 buffer read at stint pass 0
   int lastpass[kMaxGraphs];      // last pass each graph took part in during the stint
-  int cnt[2];
-  int used;
-  int rp_top;
-  int stop;
-  int need;
-  int wide;
+  // Per list, indexed by stint pass % 3: the list read by pass j is filled
+  // during pass j - 1 and its counters are cleared during pass j + 1, so a
+  // thread reading them at the top of pass j never races a writer.
+  int cnt[3];                    // entries
+  int need[3];                   // row entries still to load
+  int wide[3];                   // holds a row longer than 32 entries
+  int used;                      // vertex-table slots in use
+  int rp_top;                    // row-pool entries in use
+  int stop_at;                   // stint pass at which a time budget stops the stint
+  int stop_slice;                // that budget was the launch's time slice
 };
 
 __device__ __forceinline__ unsigned mix64(unsigned long long x) {
@@ -897,7 +970,8 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
       c.len[h] = len > kNarrowMax ? kWideLen : static_cast<unsigned char>(len);
       c.graph[h] = static_cast<unsigned short>(g);
       c.flags[h] = static_cast<unsigned char>(((s.ctl->cur_buf ^ e.recs[g].ba.pass0) & 1) << 2);
-      c.row[h] = -1;
+      c.row[h] = kNoRow;
+      c.visits[h] = 0;
       c.mark[h] = -1;
       atomicAdd(&c.used, 1);
       return static_cast<int>(h);
@@ -918,10 +992,16 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   const int grp = lane / G, gl = lane & (G - 1);
   for (int i = tid; i < kVT; i += kBlock) c.key[i] = kEmptyKey;
   for (int g = tid; g < ng; g += kBlock) c.lastpass[g] = -1;
+  if (tid < 3) {
+    c.cnt[tid] = 0;
+    c.need[tid] = 0;
+    c.wide[tid] = 0;
+  }
   if (tid == 0) {
-    c.cnt[0] = 0;
     c.used = 0;
     c.rp_top = 0;
+    c.stop_at = 0x7fffffff;
+    c.stop_slice = 0;
   }
   __syncthreads();
   int max_iter = 0x7fffffff;
@@ -934,86 +1014,94 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     const int *gl_list = r.st.flist + static_cast<size_t>((k0 + r.ba.pass0) % 3) * r.st.n;
     for (int i = lane; i < nn + nw; i += 32) {
       const int v = i < nn ? gl_list[i] : gl_list[r.st.n - 1 - (i - nn)];
-      const int slot = vt_slot(c, e, g, v);
-      c.list[0][atomicAdd(&c.cnt[0], 1)] = static_cast<unsigned short>(slot);
+      const int sl = vt_slot(c, e, g, v);
+      c.list[0][atomicAdd(&c.cnt[0], 1)] = static_cast<unsigned short>(sl);
+    }
+  }
+  int rec = 0;
+  for (int g = tid; g < ng; g += kBlock) {  // recorded sizes of the first pass are counted up below
+    const GraphRec &r = e.recs[g];
+    const int kg = k0 + r.ba.pass0;
+    rec |= r.ba.record;
+    if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
+  }
+  const bool rec_any = __syncthreads_or(rec) != 0;
+  {
+    int need = 0, wide = 0;
+    for (int i = tid; i < c.cnt[0]; i += kBlock) {
+      const int su = c.list[0][i];
+      if (c.len[su] == kWideLen) wide = 1;
+      else need += c.len[su];
+    }
+    need = __reduce_add_sync(0xffffffffu, need);
+    wide = __any_sync(0xffffffffu, wide);
+    if (lane == 0) {
+      if (need) atomicAdd(&c.need[0], need);
+      if (wide) c.wide[0] = 1;
     }
   }
   __syncthreads();
   const uint64_t t0 = global_timer_ns();
-  int k = k0, p = 0;
-  for (;; ++k, p ^= 1) {
-    const int cnt = c.cnt[p];
-    // rows still to load and their neighbours: bound the table and the pool
-    if (tid == 0) {
-      c.need = 0;
-      c.wide = 0;
-    }
-    __syncthreads();
-    int need = 0, wide = 0;
-    for (int i = tid; i < cnt; i += kBlock) {
-      const int su = c.list[p][i];
-      if (c.len[su] == kWideLen) wide = 1;
-      else if (c.row[su] < 0) need += c.len[su];
-    }
-    need = warp_sum_i(need);
-    wide = __any_sync(0xffffffffu, wide);
-    if (lane == 0) {
-      if (need) atomicAdd(&c.need, need);
-      if (wide) c.wide = 1;
-    }
-    if (tid == 0) c.cnt[p ^ 1] = 0;
-    for (int g = tid; g < ng; g += kBlock) {  // the pass's recorded size is counted up below
-      const GraphRec &r = e.recs[g];
-      const int kg = k + r.ba.pass0;
-      if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      int stop = 0;
-      if (cnt == 0 || cnt > kSoloList || k >= max_iter || c.wide) stop = 1;
-      if (c.used + c.need > kVTUse || c.rp_top + c.need > kRP) stop = 1;
-      if (((k - k0) & 63) == 63 && global_timer_ns() - t0 > kSoloBudgetNs) stop = 1;
-      if (e.pass_budget > 0 && k >= e.pass_budget) stop = 1;
-      if (((k - k0) & 15) == 15 && slice_over(e)) {
-        stop = 1;
-        e.ectl->slice_stop = stop_code(e, k);  // the grid resumes at pass k and stops there
-      }
-      c.stop = stop;
-    }
-    __syncthreads();
-    if (c.stop) break;
-    // load the rows of frontier vertices seen for the first time
-    for (int base = warp * GPW; base < cnt; base += kWarps * GPW) {
-      const int item = base + grp;
-      int su = 0, len = 0;
-      bool load = false;
-      if (item < cnt) {
-        su = c.list[p][item];
-        load = c.row[su] < 0;
-        len = c.len[su];
-      }
-      int off = 0;
-      if (load && gl == 0) off = atomicAdd(&c.rp_top, len);
-      off = __shfl_sync(0xffffffffu, off, lane & ~(G - 1));
-      if (load) {
-        const int g = c.graph[su];
-        const DevState &s = e.recs[g].st;
-        const int rs = s.full_row[static_cast<int>(c.key[su] & 0xffffffffu)];
-        for (int ee = gl; ee < len; ee += G) {
-          const int2 ent = s.act_adj[rs + ee];
-          const int ns = ent.x >= 0 ? vt_slot(c, e, g, ent.x) : -1;
-          c.rp[off + ee] = make_int2(ns, ent.y);
+  int k = k0;
+  for (;; ++k) {
+    const int j = k - k0;
+    const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
+    const int cnt = c.cnt[q];
+    const int need = c.need[q];
+    // the same decision in every thread: its inputs were last written before
+    // the previous barrier
+    if (cnt == 0 || cnt > kSoloList || k >= max_iter || c.wide[q] || j >= kSoloMaxPasses || j >= c.stop_at ||
+        (e.pass_budget > 0 && k >= e.pass_budget) || c.used + need > kVTUse || c.rp_top + need > kRP)
+      break;
+    if (need > 0) {
+      __syncthreads();  // every thread has read used / rp_top above
+      // load the rows of frontier vertices seen for the first time
+      for (int base = warp * GPW; base < cnt; base += kWarps * GPW) {
+        const int item = base + grp;
+        int su = 0, len = 0;
+        bool load = false;
+        if (item < cnt) {
+          su = c.list[p][item];
+          load = c.row[su] == kNoRow;
+          len = c.len[su];
         }
-        if (gl == 0) c.row[su] = off;
+        int off = 0;
+        if (load && gl == 0) off = atomicAdd(&c.rp_top, len);
+        off = __shfl_sync(0xffffffffu, off, lane & ~(G - 1));
+        if (load) {
+          const int g = c.graph[su];
+          const DevState &s = e.recs[g].st;
+          const int rs = s.full_row[static_cast<int>(c.key[su] & 0xffffffffu)];
+          for (int ee = gl; ee < len; ee += G) {
+            const int2 ent = s.act_adj[rs + ee];
+            const int ns = ent.x >= 0 ? vt_slot(c, e, g, ent.x) : -1;
+            c.rp[off + ee] = make_int2(ns, ent.y);
+          }
+          if (gl == 0) c.row[su] = static_cast<unsigned short>(off);
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
+    // counters of the list filled next pass, and recorded sizes of the next pass
+    if (tid == 0) {
+      const int z = (j + 2) % 3;
+      c.cnt[z] = 0;
+      c.need[z] = 0;
+      c.wide[z] = 0;
+    }
+    if (rec_any)
+      for (int g = tid; g < ng; g += kBlock) {
+        const GraphRec &r = e.recs[g];
+        const int kg = k + 1 + r.ba.pass0;
+        if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
+      }
     // the pass: every frontier row from shared memory
+    const unsigned short *cur = c.list[p];
     unsigned short *next = c.list[p ^ 1];
     for (int base = warp * GPW; base < cnt; base += kWarps * GPW) {
       const int item = base + grp;
       const bool valid = item < cnt;
-      const int su = valid ? c.list[p][item] : 0;
+      const int su = valid ? cur[item] : 0;
       const int len = valid ? c.len[su] : 0;
       const int off = valid ? c.row[su] : 0;
       const int src = valid ? (((c.flags[su] >> 2) ^ k) & 1) : 0;
@@ -1057,28 +1145,76 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
         c.lab[src ^ 1][su] = nl;
         c.flags[su] |= 3;
         changed = fabsf(nl - old) > r.ba.delta;
-        atomicAdd(&r.st.bc->aff_edges, static_cast<unsigned long long>(len));
-        atomicAdd(&r.st.bc->front_visits, 1ull);
+        ++c.visits[su];  // a slot is in a list at most once
         const int kg = k + r.ba.pass0;
         c.lastpass[g] = kg;
         if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
       }
       changed = __shfl_sync(0xffffffffu, changed, 0, G);
       // changed vertex: non-deleted, non-GT neighbours and itself
-      // (src/iterativePropagation.cu:200-216)
+      // (src/iterativePropagation.cu:200-216). All marks first, then one
+      // reservation in the next list for the whole warp.
+      unsigned fresh = 0;
+      if (changed) {
 #pragma unroll
-      for (int r = 0; r < R + 1; ++r) {
-        const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
-        if (changed && ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1)
-          next[atomicAdd(&c.cnt[p ^ 1], 1)] = static_cast<unsigned short>(ns);
+        for (int r = 0; r < R + 1; ++r) {
+          const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
+          if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
+        }
+      }
+      const int nf = __popc(fresh);
+      int add = 0, wide = 0;
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r)
+        if ((fresh >> r) & 1u) {
+          const int ns = r < R ? vv[r] : su;
+          const int l = c.len[ns];
+          if (l == kWideLen) wide = 1;
+          else if (c.row[ns] == kNoRow) add += l;
+        }
+      int incl = nf;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int tot = __shfl_sync(0xffffffffu, incl, 31);
+      add = __reduce_add_sync(0xffffffffu, add);
+      wide = __reduce_or_sync(0xffffffffu, wide);
+      int at = 0;
+      if (lane == 31 && tot) {
+        at = atomicAdd(&c.cnt[nq], tot);
+        if (add) atomicAdd(&c.need[nq], add);
+        if (wide) c.wide[nq] = 1;
+      }
+      at = __shfl_sync(0xffffffffu, at, 31) + incl - nf;
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r)
+        if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
+    }
+    // time budgets: checked by thread 0, they stop the stint two passes on
+    // (a thread still at the top of this pass must not see the request)
+    if (tid == 0 && (j & 15) == 15) {
+      if (global_timer_ns() - t0 > kSoloBudgetNs) c.stop_at = j + 1;
+      if (slice_over(e)) {
+        c.stop_at = j + 1;
+        c.stop_slice = 1;
       }
     }
     __syncthreads();
   }
-  // labels written during the stint go back to HBM
+  if (tid == 0 && c.stop_slice) e.ectl->slice_stop = stop_code(e, k);  // the grid resumes at pass k and stops
+  const int jq = (k - k0) % 3, jp = (k - k0) & 1;
+  // labels written during the stint go back to HBM, with the visit counts
   for (int i = tid; i < kVT; i += kBlock) {
-    if (c.key[i] == kEmptyKey || !(c.flags[i] & 1)) continue;
+    if (c.key[i] == kEmptyKey) continue;
     const DevState &s = e.recs[c.graph[i]].st;
+    const int vis = c.visits[i];
+    if (vis) {
+      atomicAdd(&s.bc->aff_edges, static_cast<unsigned long long>(vis) * c.len[i]);
+      atomicAdd(&s.bc->front_visits, static_cast<unsigned long long>(vis));
+    }
+    if (!(c.flags[i] & 1)) continue;
     const int v = static_cast<int>(c.key[i] & 0xffffffffu);
     s.lab0[v] = c.lab[0][i];
     s.lab1[v] = c.lab[1][i];
@@ -1093,9 +1229,9 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     bc->front_count[(kg + 1) % 3][0] = bc->front_count[(kg + 1) % 3][1] = 0;
   }
   __syncthreads();
-  const int cnt = c.cnt[p];
+  const int cnt = c.cnt[jq];
   for (int i = tid; i < cnt; i += kBlock) {
-    const int su = c.list[p][i];
+    const int su = c.list[jp][i];
     const GraphRec &r = e.recs[c.graph[su]];
     const DevState &s = r.st;
     const int v = static_cast<int>(c.key[su] & 0xffffffffu);
@@ -1160,17 +1296,11 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
     const unsigned stamp = w.g0 + static_cast<unsigned>(kg) + 1u;
     const int u = valid ? s.flist[static_cast<size_t>(kg % 3) * s.n + (item - pref[g])] : 0;
-    auto mark = [&](bool cand, int v) {
-      bool fresh = false, first = false;
-      if (cand) {
-        const unsigned old = atomicMax(&s.front_stamp[v], stamp);
-        fresh = old < stamp;
-        first = old < w.g0;
-      }
-      frontier_append(w, fresh, first, v, nset);
-    };
     int len = 0;
-    narrow_row<G>(s, src, dst, w.a.delta, u, valid, gl, len, mark);
+    int cand[32 / G + 1];
+    unsigned wide_bits = 0;
+    narrow_row<G>(s, src, dst, w.a.delta, u, valid, gl, len, cand, wide_bits);
+    group_mark<G>(w, cand, wide_bits, stamp, nset, gl);
     add_keyed(valid && gl == 0, static_cast<unsigned>(len), &s.bc->aff_edges);
     add_keyed(valid && gl == 0, 1u, &s.bc->front_visits);
   }
@@ -1269,7 +1399,7 @@ __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2
                         k != no_small_at;
     if (solo_ok || sub_ok) {
       if (solo_ok) {
-        if (blockIdx.x == 0) solo_passes<G>(e, k, stint & 1, solo);
+        if (blockIdx.x == 0) solo_passes<kSoloG>(e, k, stint & 1, solo);
       } else if (blockIdx.x < kSubBlocks) {
         if (!sub_passes<G>(e, k, stint & 1, pref, pref2)) return false;
       }

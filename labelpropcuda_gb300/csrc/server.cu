@@ -155,10 +155,8 @@ struct dlp_server {
     return DLP_OK;
   }
 
-  // Copies a request's arrays to its graph's device buffer (on the engine's
-  // stream, ahead of the step's launch) and returns the device view.
-  int stage(Request &r, GraphBuf &b, dlp_batch_view *out) {
-    const size_t total = std::max<size_t>(r.batch_bytes, 16);
+  // Grows a graph's staging buffers (pinned and device) to hold `total` bytes.
+  int grow(GraphBuf &b, size_t total) {
     cudaStream_t s = static_cast<cudaStream_t>(dlp_engine_stream(eng));
     if (total > b.pin_cap) {
       if (b.pinned) cudaFreeHost(b.pinned);
@@ -175,6 +173,15 @@ struct dlp_server {
       DLP_CUDA_TRY(cudaMalloc(&b.dev, total * 2));
       b.dev_cap = total * 2;
     }
+    return DLP_OK;
+  }
+
+  // Copies a request's arrays to its graph's device buffer (on the engine's
+  // stream, ahead of the step's launch) and returns the device view.
+  int stage(Request &r, GraphBuf &b, dlp_batch_view *out) {
+    const size_t total = std::max<size_t>(r.batch_bytes, 16);
+    cudaStream_t s = static_cast<cudaStream_t>(dlp_engine_stream(eng));
+    DLP_TRY(grow(b, total));
     size_t off = 0;
     auto put = [&](const void *src, size_t bytes) {
       if (bytes) std::memcpy(b.pinned + off, src, bytes);
@@ -344,6 +351,21 @@ int dlp_server_destroy(dlp_server *s) {
 }
 
 double dlp_server_clock(const dlp_server *s) { return s ? s->now() : 0.0; }
+
+int dlp_server_reserve(dlp_server *s, int graph_id, int max_inserted, int max_gt, int max_deleted, int max_edges) {
+  dlp::clear_error();
+  if (!s || max_inserted < 0 || max_gt < 0 || max_deleted < 0 || max_edges < 0)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null server or negative size");
+  if (dlp_engine_graph_nodes(s->eng, graph_id) <= 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph id");
+  dlp_batch_view v{};
+  v.num_inserted = max_inserted;
+  v.num_gt = max_gt;
+  v.num_deleted = max_deleted;
+  v.num_edges = max_edges;
+  const size_t total = std::max<size_t>(batch_bytes(v), 16);
+  DLP_TRY(s->grow(s->buf(graph_id), (total + 1) / 2));  // grow() keeps twice what it is asked for
+  return dlp_engine_reserve(s->eng, graph_id, max_edges, max_deleted);
+}
 
 int dlp_server_submit(dlp_server *s, const dlp_request *req, int *request_id) {
   dlp::clear_error();
