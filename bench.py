@@ -386,7 +386,12 @@ def served_block(args, local_rank) -> dict:
     t_setup = time.perf_counter()
     specs = mix_sizes(args.served_graphs, 1e3, 5e5, 1000003)
     probs = make_problems(specs, min(16, os.cpu_count() or 1))
-    eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=args.served_lanes)
+    lanes, bps, tune = args.served_lanes, 0, None
+    if lanes == 0:  # autotune the launch shape on a sample of the same size distribution
+        sample = specs[:: max(1, len(specs) // 8)][:8]
+        tune = dlp.autotune([s[0] for s in sample], [s[1] for s in sample], batches=10, max_iterations=300)
+        lanes, bps = tune["narrow_lanes"], tune["blocks_per_sm"]
+    eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=lanes, blocks_per_sm=bps)
     gids = [eng.add_problem(p) for p in probs]
     nb = 10
     for g, p in zip(gids, probs):  # scratch sized up front: no allocation inside the timed runs
@@ -481,7 +486,8 @@ def served_block(args, local_rank) -> dict:
            "served_poisson": served_poisson, "plain": plain,
            "served_over_plain": served_sat["value"] / plain_v if plain_v else None,
            "batched_over_plain": batched["value"] / plain_v if plain_v else None,
-           "slice_us": args.slice_us, "narrow_lanes": args.served_lanes}
+           "slice_us": args.slice_us, "narrow_lanes": lanes, "blocks_per_sm": bps or "occupancy",
+           "autotune": tune}
     eng.close()
     return out
 
@@ -498,7 +504,7 @@ def main(argv=None) -> int:
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--ref-budget-s", type=float, default=20.0)
     ap.add_argument("--served-graphs", type=int, default=64)
-    ap.add_argument("--served-lanes", type=int, default=4)
+    ap.add_argument("--served-lanes", type=int, default=0, help="0: autotune")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--slice-us", type=float, default=1000.0)
     ap.add_argument("--plain-budget-s", type=float, default=20.0)

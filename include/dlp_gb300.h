@@ -209,6 +209,17 @@ int dlp_engine_add_graph(dlp_engine *e, int num_nodes, int64_t num_edges, const 
                          const int *vertex_batch_map, int *graph_id);
 /* Frees a graph's device memory (eviction); its id becomes free. */
 int dlp_engine_remove_graph(dlp_engine *e, int graph_id);
+/* Copies a graph's whole device state (graph, labels, live rows, counters,
+ * the statistics kept so far) to host memory, so that it can be evicted with
+ * dlp_engine_remove_graph and brought back later by dlp_engine_restore with
+ * identical results. With out == NULL, *bytes receives the size needed. Not
+ * allowed while the graph's batch is in progress. No counterpart in the
+ * reference (its graph state lives in its driver loop only). */
+int dlp_engine_snapshot(dlp_engine *e, int graph_id, void *out, size_t capacity, size_t *bytes);
+/* Makes a snapshotted graph resident again, in this or another engine with
+ * the same record flag and semantics; counts against the memory budget like
+ * dlp_engine_add_graph. *graph_id receives its (possibly new) id. */
+int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *graph_id);
 int dlp_engine_reset_graph(dlp_engine *e, int graph_id);
 float dlp_engine_tau(const dlp_engine *e, int graph_id);
 void *dlp_engine_stream(dlp_engine *e);
@@ -235,6 +246,26 @@ int dlp_engine_elapsed_ms(dlp_engine *e, int first_step, int last_step, float *m
 int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels);
 int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, int64_t capacity,
                         int64_t *count);
+
+/* Autotuner (no counterpart in the reference, whose launch shapes are fixed).
+ * Propagation sends rows of at most 32 live entries to groups of
+ * narrow_lanes lanes and longer rows to whole warps; the lane width of that
+ * short-row bucket and the persistent grid's blocks per SM are chosen by
+ * timing every candidate (lanes 4/8/16 x 2 or 1 blocks per SM) on a sample the
+ * library generates with the reference generator: num_graphs graphs of
+ * sizes[i] vertices and average degree degrees[i], `batches` batches each,
+ * propagation capped at max_iterations passes per batch for the trial. Every
+ * candidate must give identical statistics (checked). The fastest is written
+ * into cfg->narrow_lanes and cfg->blocks_per_sm; other fields are kept. */
+typedef struct {
+  int candidates;
+  int best;               /* index of the chosen candidate */
+  int lanes[8];
+  int blocks_per_sm[8];
+  double ms[8];           /* summed device time of the sample's steps */
+} dlp_tune_report;
+int dlp_autotune(dlp_config *cfg, int num_graphs, const int *sizes, const int *degrees, int batches,
+                 int max_iterations, dlp_tune_report *report);
 
 /* ------------------------------------------------------------------------ */
 /* 2c. Continuous batching (no counterpart in the reference, which applies   */

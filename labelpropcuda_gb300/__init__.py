@@ -259,6 +259,22 @@ class Engine:
     def reset_graph(self, gid: int) -> None:
         _n.check(_n.lib().dlp_engine_reset_graph(self._h, gid))
 
+    def snapshot(self, gid: int) -> bytes:
+        """The graph's whole device state as bytes (for eviction)."""
+        L = _n.lib()
+        size = ctypes.c_size_t(0)
+        _n.check(L.dlp_engine_snapshot(self._h, gid, None, 0, ctypes.byref(size)))
+        buf = ctypes.create_string_buffer(size.value)
+        _n.check(L.dlp_engine_snapshot(self._h, gid, buf, size.value, ctypes.byref(size)))
+        return buf.raw
+
+    def restore(self, snap: bytes) -> int:
+        """Makes a snapshotted graph resident again; returns its id."""
+        gid = ctypes.c_int(-1)
+        _n.check(_n.lib().dlp_engine_restore(self._h, snap, len(snap), ctypes.byref(gid)))
+        self.sizes[gid.value] = int(_n.lib().dlp_engine_graph_nodes(self._h, gid.value))
+        return gid.value
+
     def tau(self, gid: int) -> float:
         return float(_n.lib().dlp_engine_tau(self._h, gid))
 
@@ -341,6 +357,26 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+def autotune(sizes: list[int], degrees: list[int], batches: int = 10, max_iterations: int = 2000,
+             **config) -> dict:
+    """Times every launch-shape candidate (lanes per short row x blocks per
+    SM) on a generated sample of the given graph sizes and degrees and
+    returns the fastest as {"narrow_lanes", "blocks_per_sm", "candidates"}."""
+    L = _n.lib()
+    cfg = _n.Config()
+    L.dlp_config_default(ctypes.byref(cfg))
+    for k, v in config.items():
+        setattr(cfg, k, v)
+    n = len(sizes)
+    sz = (ctypes.c_int * n)(*sizes)
+    dg = (ctypes.c_int * n)(*degrees)
+    rep = _n.TuneReport()
+    _n.check(L.dlp_autotune(ctypes.byref(cfg), n, sz, dg, batches, max_iterations, ctypes.byref(rep)))
+    cands = [{"narrow_lanes": rep.lanes[i], "blocks_per_sm": rep.blocks_per_sm[i], "ms": rep.ms[i]}
+             for i in range(rep.candidates)]
+    return {"narrow_lanes": cfg.narrow_lanes, "blocks_per_sm": cfg.blocks_per_sm, "candidates": cands}
 
 
 class Server:

@@ -75,6 +75,13 @@ class RequestResult(ctypes.Structure):
     ]
 
 
+class TuneReport(ctypes.Structure):
+    _fields_ = [
+        ("candidates", ctypes.c_int), ("best", ctypes.c_int), ("lanes", ctypes.c_int * 8),
+        ("blocks_per_sm", ctypes.c_int * 8), ("ms", ctypes.c_double * 8),
+    ]
+
+
 # status codes
 DLP_OK = 0
 DLP_ERR_INVALID_ARGUMENT = 1
@@ -152,6 +159,9 @@ _SIGNATURES = {
     "dlp_engine_step_sliced": (_I, [_P, _I, _P, _P, ctypes.POINTER(BatchView), _I, ctypes.c_double, c_int_p, c_int_p,
                                     c_int_p]),
     "dlp_engine_graph_nodes": (_I, [_P, _I]),
+    "dlp_engine_snapshot": (_I, [_P, _I, _P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "dlp_engine_restore": (_I, [_P, _P, ctypes.c_size_t, c_int_p]),
+    "dlp_autotune": (_I, [ctypes.POINTER(Config), _I, c_int_p, c_int_p, _I, _I, ctypes.POINTER(TuneReport)]),
     "dlp_engine_reserve": (_I, [_P, _I, _I, _I]),
     "dlp_server_reserve": (_I, [_P, _I, _I, _I, _I, _I]),
     "dlp_engine_in_progress": (_I, [_P, _I]),

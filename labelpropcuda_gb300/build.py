@@ -33,7 +33,7 @@ NVCC_FLAGS = ARCH + [
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-I/usr/local/cuda/include",
              f"-I{INCLUDE}", f"-I{CSRC}"]
 
-CU_SOURCES = ["api.cu", "engine.cu", "engine_kernel.cu", "launchers.cu", "server.cu"]
+CU_SOURCES = ["api.cu", "engine.cu", "engine_kernel.cu", "launchers.cu", "server.cu", "tune.cu"]
 CXX_SOURCES = ["host/generate.cpp", "shims.cpp"]
 CLI_SOURCES = ["cli/main.cpp"]
 

@@ -46,7 +46,8 @@ __global__ void fill_f32_kernel(float *p, float v, int64_t count) {
 
 size_t align16(size_t x) { return (x + 15) & ~static_cast<size_t>(15); }
 
-int dalloc_bytes(void **p, size_t bytes, std::vector<void *> &owned, size_t &counted) {
+int dalloc_bytes(void **p, size_t bytes, std::vector<void *> &owned, size_t &counted,
+                 std::vector<size_t> *sizes = nullptr) {
   void *q = nullptr;
   bytes = std::max<size_t>(bytes, 16);
   cudaError_t e = cudaMalloc(&q, bytes);
@@ -56,15 +57,16 @@ int dalloc_bytes(void **p, size_t bytes, std::vector<void *> &owned, size_t &cou
                      std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
   }
   owned.push_back(q);
+  if (sizes) sizes->push_back(bytes);
   counted += bytes;
   *p = q;
   return DLP_OK;
 }
 
 template <class T>
-int dalloc(T **p, size_t count, std::vector<void *> &owned, size_t &counted) {
+int dalloc(T **p, size_t count, std::vector<void *> &owned, size_t &counted, std::vector<size_t> *sizes = nullptr) {
   void *q = nullptr;
-  DLP_TRY(dalloc_bytes(&q, count * sizeof(T), owned, counted));
+  DLP_TRY(dalloc_bytes(&q, count * sizeof(T), owned, counted, sizes));
   *p = static_cast<T *>(q);
   return DLP_OK;
 }
@@ -84,6 +86,8 @@ struct GraphSlot {
   int64_t m = 0;
   float tau = 0.5f;
   std::vector<void *> owned;
+  std::vector<size_t> sizes;  // bytes of each owned array, in allocation order
+  bool has_truth = false, has_bmap = false;
   size_t bytes = 0;
   DevState st{};
   dlp_batch_stats *stats = nullptr;  // ring of kStepRing
@@ -104,6 +108,7 @@ struct GraphSlot {
   void free_all() {
     for (void *p : owned) cudaFree(p);
     owned.clear();
+    sizes.clear();
     for (void *p : {static_cast<void *>(lsrc), static_cast<void *>(ldst), static_cast<void *>(sub_pairs),
                     static_cast<void *>(sub_local), static_cast<void *>(del_pre), static_cast<void *>(del_keep)})
       cudaFree(p);
@@ -480,6 +485,53 @@ int stage_step(dlp_engine *e, int count, const int *gids, const dlp_batch_view *
   return DLP_OK;
 }
 
+// Allocates every device array of a graph of n vertices and m directed edges
+// (always in the same order: snapshots rely on it) for graph id gid.
+int alloc_graph(dlp_engine *e, int n, int64_t m, bool with_truth, bool with_bmap, int gid, GraphSlot **out) {
+  GraphSlot *g = new GraphSlot();
+  g->n = n;
+  g->m = m;
+  g->has_truth = with_truth;
+  g->has_bmap = with_bmap;
+  DevState &d = g->st;
+  d.n = n;
+  int *full_row = nullptr;
+  int2 *full_adj = nullptr;
+  uint8_t *truth = nullptr;
+  int *bmap = nullptr;
+  auto &o = g->owned;
+  size_t &b = g->bytes;
+  std::vector<size_t> *z = &g->sizes;
+  int st = DLP_OK;
+  if ((st = dalloc(&full_row, n + 1, o, b, z)) || (st = dalloc(&full_adj, m, o, b, z)) ||
+      (st = dalloc(&d.act_adj, m, o, b, z)) || (st = dalloc(&d.act_len, n, o, b, z)) ||
+      (st = dalloc(&d.status, n, o, b, z)) || (st = dalloc(&d.gt, n, o, b, z)) ||
+      (st = dalloc(&d.contrib, n, o, b, z)) || (st = dalloc(&d.lab0, n, o, b, z)) ||
+      (st = dalloc(&d.lab1, n, o, b, z)) || (st = dalloc(&d.local, n, o, b, z)) ||
+      (st = dalloc(&d.del_stamp, n, o, b, z)) || (st = dalloc(&d.gt_stamp, n, o, b, z)) ||
+      (st = dalloc(&d.dirty_stamp, n, o, b, z)) || (st = dalloc(&d.front_stamp, n, o, b, z)) ||
+      (st = dalloc(&d.dirty_list, n, o, b, z)) || (st = dalloc(&d.seed_list, n, o, b, z)) ||
+      (st = dalloc(&d.flist, 3 * static_cast<size_t>(n), o, b, z)) ||
+      (st = dalloc(&d.touched, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&d.par, n, o, b, z)) ||
+      (st = dalloc(&d.acc, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&g->stats, kStepRing, o, b, z)) ||
+      (with_truth && (st = dalloc(&truth, n, o, b, z))) || (with_bmap && (st = dalloc(&bmap, n, o, b, z))) ||
+      (e->cfg.record &&
+       ((st = dalloc(&d.rec_front0, n, o, b, z)) || (st = dalloc(&d.rec_root, n, o, b, z)) ||
+        (st = dalloc(&d.rec_init, n, o, b, z)) || (st = dalloc(&d.rec_fsizes, dlp::session::kRecordIters, o, b, z)) ||
+        (st = dalloc(&d.rec_minid, n, o, b, z))))) {
+    g->free_all();
+    delete g;
+    return st;
+  }
+  d.full_row = full_row;
+  d.full_adj = full_adj;
+  d.truth = truth;
+  d.batch_map = bmap;
+  d.ctl = e->ctl_all + gid;
+  *out = g;
+  return DLP_OK;
+}
+
 int find_seq(GraphSlot *g, int batch) {
   for (int q = static_cast<int>(g->seq_batch.size()) - 1; q >= 0; --q)
     if (g->seq_batch[q] == batch) return q;
@@ -608,9 +660,8 @@ int dlp_engine_add_graph(dlp_engine *e, int n, int64_t m, const int *row_ptr, co
     }
   if (gid < 0) return dlp::fail(DLP_ERR_OUT_OF_MEMORY, "the engine holds max_graphs graphs already");
   DLP_CUDA_TRY(cudaSetDevice(e->device));
-  GraphSlot *g = new GraphSlot();
-  g->n = n;
-  g->m = m;
+  GraphSlot *g = nullptr;
+  DLP_TRY(alloc_graph(e, n, m, true_labels != nullptr, vertex_batch_map != nullptr, gid, &g));
   g->tau = e->cfg.tau < 0.0f ? dlp_mean_edge_weight(m, col_ind, values) : e->cfg.tau;
   auto bail = [&](int st) {
     g->free_all();
@@ -618,38 +669,11 @@ int dlp_engine_add_graph(dlp_engine *e, int n, int64_t m, const int *row_ptr, co
     return st;
   };
   DevState &d = g->st;
-  d.n = n;
-  int *full_row = nullptr;
-  int2 *full_adj = nullptr;
-  uint8_t *truth = nullptr;
-  int *bmap = nullptr;
-  auto &o = g->owned;
-  size_t &b = g->bytes;
+  int *full_row = const_cast<int *>(d.full_row);
+  int2 *full_adj = const_cast<int2 *>(d.full_adj);
+  uint8_t *truth = const_cast<uint8_t *>(d.truth);
+  int *bmap = const_cast<int *>(d.batch_map);
   int st = DLP_OK;
-  if ((st = dalloc(&full_row, n + 1, o, b)) || (st = dalloc(&full_adj, m, o, b)) ||
-      (st = dalloc(&d.act_adj, m, o, b)) || (st = dalloc(&d.act_len, n, o, b)) ||
-      (st = dalloc(&d.status, n, o, b)) || (st = dalloc(&d.gt, n, o, b)) || (st = dalloc(&d.contrib, n, o, b)) ||
-      (st = dalloc(&d.lab0, n, o, b)) || (st = dalloc(&d.lab1, n, o, b)) || (st = dalloc(&d.local, n, o, b)) ||
-      (st = dalloc(&d.del_stamp, n, o, b)) || (st = dalloc(&d.gt_stamp, n, o, b)) ||
-      (st = dalloc(&d.dirty_stamp, n, o, b)) || (st = dalloc(&d.front_stamp, n, o, b)) ||
-      (st = dalloc(&d.dirty_list, n, o, b)) || (st = dalloc(&d.seed_list, n, o, b)) ||
-      (st = dalloc(&d.flist, 3 * static_cast<size_t>(n), o, b)) ||
-      (st = dalloc(&d.touched, 2 * static_cast<size_t>(n), o, b)) || (st = dalloc(&d.par, n, o, b)) ||
-      (st = dalloc(&d.acc, 2 * static_cast<size_t>(n), o, b)) || (st = dalloc(&g->stats, kStepRing, o, b)))
-    return bail(st);
-  if (true_labels && (st = dalloc(&truth, n, o, b))) return bail(st);
-  if (vertex_batch_map && (st = dalloc(&bmap, n, o, b))) return bail(st);
-  if (e->cfg.record) {
-    if ((st = dalloc(&d.rec_front0, n, o, b)) || (st = dalloc(&d.rec_root, n, o, b)) ||
-        (st = dalloc(&d.rec_init, n, o, b)) || (st = dalloc(&d.rec_fsizes, dlp::session::kRecordIters, o, b)) ||
-        (st = dalloc(&d.rec_minid, n, o, b)))
-      return bail(st);
-  }
-  d.full_row = full_row;
-  d.full_adj = full_adj;
-  d.truth = truth;
-  d.batch_map = bmap;
-  d.ctl = e->ctl_all + gid;
   auto up = [&](void *dst, const void *src, size_t bytes) -> int {
     if (bytes == 0) return DLP_OK;
     DLP_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
@@ -700,6 +724,140 @@ int dlp_engine_remove_graph(dlp_engine *e, int graph_id) {
   g->free_all();
   delete g;
   e->graphs[graph_id] = nullptr;
+  return DLP_OK;
+}
+
+// Snapshot layout: SnapHeader, the byte size of each device array (uint64),
+// SessionCtl, BatchCounters, the arrays in allocation order, the previous
+// batch's deletions (int32[prev_d]) and the batch index of every applied
+// batch (int32[seq]).
+namespace {
+constexpr uint64_t kSnapMagic = 0x31504e5350444c44ull;  // "DLDPSNP1"
+struct SnapHeader {
+  uint64_t magic;
+  int64_t m;
+  int n, truth, bmap, record, semantics, narrays, seq, prev_d, last_inserted;
+  float tau;
+};
+
+size_t snapshot_bytes(const GraphSlot *g) {
+  size_t b = sizeof(SnapHeader) + sizeof(uint64_t) * g->sizes.size() + sizeof(SessionCtl) + sizeof(BatchCounters);
+  for (size_t z : g->sizes) b += z;
+  return b + sizeof(int) * (static_cast<size_t>(g->prev_d) + g->seq);
+}
+}  // namespace
+
+int dlp_engine_snapshot(dlp_engine *e, int graph_id, void *out, size_t capacity, size_t *bytes) {
+  dlp::clear_error();
+  GraphSlot *g = slot_of(e, graph_id);
+  if (!g || !bytes) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph or null bytes");
+  if (g->inflight) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "the graph's batch is still in progress");
+  const size_t need = snapshot_bytes(g);
+  *bytes = need;
+  if (!out) return DLP_OK;
+  if (capacity < need) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "snapshot buffer too small");
+  DLP_CUDA_TRY(cudaSetDevice(e->device));
+  DLP_CUDA_TRY(cudaStreamSynchronize(e->stream));
+  char *p = static_cast<char *>(out);
+  SnapHeader h{};
+  h.magic = kSnapMagic;
+  h.m = g->m;
+  h.n = g->n;
+  h.truth = g->has_truth;
+  h.bmap = g->has_bmap;
+  h.record = e->cfg.record != 0;
+  h.semantics = e->cfg.semantics;
+  h.narrays = static_cast<int>(g->sizes.size());
+  h.seq = g->seq;
+  h.prev_d = g->prev_d;
+  h.last_inserted = g->last_inserted;
+  h.tau = g->tau;
+  std::memcpy(p, &h, sizeof(h));
+  p += sizeof(h);
+  for (size_t z : g->sizes) {
+    const uint64_t v = z;
+    std::memcpy(p, &v, sizeof(v));
+    p += sizeof(v);
+  }
+  DLP_CUDA_TRY(cudaMemcpy(p, e->ctl_all + graph_id, sizeof(SessionCtl), cudaMemcpyDeviceToHost));
+  p += sizeof(SessionCtl);
+  DLP_CUDA_TRY(cudaMemcpy(p, e->bc_all + graph_id, sizeof(BatchCounters), cudaMemcpyDeviceToHost));
+  p += sizeof(BatchCounters);
+  for (size_t i = 0; i < g->owned.size(); ++i) {
+    DLP_CUDA_TRY(cudaMemcpy(p, g->owned[i], g->sizes[i], cudaMemcpyDeviceToHost));
+    p += g->sizes[i];
+  }
+  if (g->prev_d > 0) DLP_CUDA_TRY(cudaMemcpy(p, g->del_keep, sizeof(int) * g->prev_d, cudaMemcpyDeviceToHost));
+  p += sizeof(int) * g->prev_d;
+  if (g->seq > 0) std::memcpy(p, g->seq_batch.data(), sizeof(int) * g->seq);
+  return DLP_OK;
+}
+
+int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *graph_id) {
+  dlp::clear_error();
+  if (!e || !snapshot || !graph_id) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+  *graph_id = -1;
+  SnapHeader h{};
+  if (bytes < sizeof(h)) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "snapshot too short");
+  std::memcpy(&h, snapshot, sizeof(h));
+  if (h.magic != kSnapMagic) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "not a graph snapshot");
+  if (h.record != (e->cfg.record != 0) || h.semantics != e->cfg.semantics)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "snapshot was taken by an engine with other settings");
+  if (h.n <= 0 || h.m < 0 || h.seq < 0 || h.prev_d < 0 || h.narrays <= 0)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "corrupt snapshot header");
+  const size_t need = graph_bytes(h.n, h.m, h.truth != 0, h.bmap != 0, h.record != 0);
+  if (e->budget > 0 && e->used + need > e->budget)
+    return dlp::fail(DLP_ERR_OUT_OF_MEMORY, "graph does not fit the engine's device-memory budget");
+  int gid = -1;
+  for (int i = 0; i < e->max_graphs; ++i)
+    if (!e->graphs[i]) {
+      gid = i;
+      break;
+    }
+  if (gid < 0) return dlp::fail(DLP_ERR_OUT_OF_MEMORY, "the engine holds max_graphs graphs already");
+  DLP_CUDA_TRY(cudaSetDevice(e->device));
+  GraphSlot *g = nullptr;
+  DLP_TRY(alloc_graph(e, h.n, h.m, h.truth != 0, h.bmap != 0, gid, &g));
+  auto bail = [&](int st) {
+    g->free_all();
+    delete g;
+    return st;
+  };
+  if (static_cast<int>(g->sizes.size()) != h.narrays)
+    return bail(dlp::fail(DLP_ERR_INVALID_ARGUMENT, "snapshot layout does not match this build"));
+  const char *p = static_cast<const char *>(snapshot) + sizeof(h);
+  for (size_t z : g->sizes) {
+    uint64_t v = 0;
+    std::memcpy(&v, p, sizeof(v));
+    p += sizeof(v);
+    if (v != z) return bail(dlp::fail(DLP_ERR_INVALID_ARGUMENT, "snapshot layout does not match this build"));
+  }
+  g->tau = h.tau;
+  g->seq = h.seq;
+  g->last_inserted = h.last_inserted;
+  g->prev_d = h.prev_d;  // del_keep is still null, so growing it below copies nothing
+  if (bytes < snapshot_bytes(g)) return bail(dlp::fail(DLP_ERR_INVALID_ARGUMENT, "snapshot too short"));
+  int st = DLP_OK;
+  auto up = [&](void *dst, const void *src, size_t n) -> int {
+    DLP_CUDA_TRY(cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice));
+    return DLP_OK;
+  };
+  if ((st = up(e->ctl_all + gid, p, sizeof(SessionCtl)))) return bail(st);
+  p += sizeof(SessionCtl);
+  if ((st = up(e->bc_all + gid, p, sizeof(BatchCounters)))) return bail(st);
+  p += sizeof(BatchCounters);
+  for (size_t i = 0; i < g->owned.size(); ++i) {
+    if ((st = up(g->owned[i], p, g->sizes[i]))) return bail(st);
+    p += g->sizes[i];
+  }
+  if ((st = grow_graph_scratch(e, g, 0, h.prev_d))) return bail(st);
+  if (h.prev_d > 0 && (st = up(g->del_keep, p, sizeof(int) * h.prev_d))) return bail(st);
+  p += sizeof(int) * h.prev_d;
+  g->seq_batch.assign(reinterpret_cast<const int *>(p), reinterpret_cast<const int *>(p) + h.seq);
+  g->seq_step.assign(h.seq, -1);
+  e->graphs[gid] = g;
+  e->used += g->bytes;
+  *graph_id = gid;
   return DLP_OK;
 }
 
@@ -805,9 +963,9 @@ int dlp_engine_stats(dlp_engine *e, int graph_id, int batch_index, dlp_batch_sta
   DLP_CUDA_TRY(cudaStreamSynchronize(e->stream));
   DLP_TRY(device_error(e));
   DLP_CUDA_TRY(cudaMemcpy(out, g->stats + (seq % kStepRing), sizeof(*out), cudaMemcpyDeviceToHost));
-  const int step = g->seq_step[seq];
+  const int step = g->seq_step[seq];  // -1 for a batch applied before a restore
   float ms = 0.0f;
-  if (e->steps - step <= kStepRing &&
+  if (step >= 0 && e->steps - step <= kStepRing &&
       cudaEventElapsedTime(&ms, e->ev[step % kStepRing][0], e->ev[step % kStepRing][1]) == cudaSuccess)
     out->device_ms = ms;
   else

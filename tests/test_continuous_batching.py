@@ -190,3 +190,35 @@ def test_server_submit_poll_and_memory_budget(gpu):
     rid = tiny.submit(gids[0], 0, probs[0].batches[1])
     assert tiny.poll() == [rid]
     assert tiny.result(rid)["status"] == N.DLP_ERR_OUT_OF_MEMORY
+
+
+@pytest.mark.gpu
+def test_snapshot_evict_restore_continues_identically(gpu):
+    """A graph snapshotted after some batches, evicted, and restored (into
+    another engine, under another id) continues exactly as if it had stayed."""
+    p = dlp.Problem(5000, 5, 10, 42)
+    want = alone(p)
+    a = dlp.Engine(4, max_iterations=MAX_ITER)
+    filler = a.add_problem(dlp.Problem(1000, 3, 5, 7))
+    gid = a.add_problem(p)
+    for b in range(4):
+        a.step([(gid, b, p.batches[b])])
+    snap = a.snapshot(gid)
+    used = a.bytes_in_use
+    a.remove_graph(gid)
+    assert a.bytes_in_use < used
+    other = dlp.Engine(2, max_iterations=MAX_ITER)
+    other.add_problem(dlp.Problem(2000, 7, 6, 3))
+    g2 = other.restore(snap)
+    assert other.stats(g2, 3)["iterations"] == want[3][0]["iterations"]  # kept statistics travel along
+    assert other.labels(g2).tobytes() == want[3][1].tobytes()
+    for b in range(4, len(p.batches)):
+        st = other.step([(g2, b, p.batches[b])])[0]
+        same(st, want[b][0], ("restored", b))
+        assert other.labels(g2).tobytes() == want[b][1].tobytes()
+    # the engine it left keeps working, and a restore into it works too
+    g3 = a.restore(snap)
+    same(a.step([(g3, 4, p.batches[4])])[0], want[4][0], ("back", 4))
+    a.step([(filler, 0, dlp.Problem(1000, 3, 5, 7).batches[0])])
+    with pytest.raises(dlp.DlpError):
+        dlp.Engine(1, max_iterations=MAX_ITER, semantics=dlp.SEMANTICS_SPEC).restore(snap)

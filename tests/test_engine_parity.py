@@ -81,3 +81,15 @@ def test_budget_admission_and_removal(gpu):
     g1 = eng.add_problem(p)
     st = eng.step([(g1, 0, p.batches[0])])
     assert st[0]["status"] == 0
+
+
+@pytest.mark.gpu
+def test_autotune_picks_a_measured_candidate(gpu):
+    """The tuner times every launch shape on a generated sample; all of them
+    must agree on the statistics (checked inside) and the choice is the
+    fastest measured one."""
+    r = dlp.autotune([3000, 1000, 2000], [5, 3, 7], batches=5, max_iterations=300)
+    assert len(r["candidates"]) == 6
+    assert all(c["ms"] > 0 for c in r["candidates"])
+    best = min(r["candidates"], key=lambda c: c["ms"])
+    assert (r["narrow_lanes"], r["blocks_per_sm"]) == (best["narrow_lanes"], best["blocks_per_sm"])
