@@ -56,9 +56,10 @@ WORKLOADS = {
 }
 
 
-def workload_desc(name: str) -> str:
+def workload_desc(name: str, limit: int = 0) -> str:
     w = WORKLOADS[name]
-    return (f"{name}: plain per-batch replay, n={w['n']}, avg degree {w['degree']}, {w['batches']} batches "
+    nb = f"first {limit} of {w['batches']}" if 0 < limit < w["batches"] else str(w["batches"])
+    return (f"{name}: plain per-batch replay, n={w['n']}, avg degree {w['degree']}, {nb} batches "
             f"(90/1/9 insert/GT/delete), delta 1e-4, maxIter 1e5, tau = mean edge weight, seed {w['seed']}")
 
 
@@ -209,6 +210,8 @@ def reference_arm(args, td, rank):
         return 0
     w = WORKLOADS[args.workload]
     p = dlp.Problem(w["n"], w["degree"], w["batches"], w["seed"])
+    if args.batches > 0:
+        p.batches = p.batches[:args.batches]
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_run(p, threads, args.ref_budget_s)
@@ -227,7 +230,7 @@ def reference_arm(args, td, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic (reference generator decisions, seed 42)",
-            "config": {"workload": workload_desc(args.workload), "semantics": "ref"},
+            "config": {"workload": workload_desc(args.workload, args.batches), "semantics": "ref"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -243,6 +246,8 @@ def gpu_arm(args, td, rank, world, local_rank):
     dlp._n.check(L.dlp_set_device(local_rank))
     w = WORKLOADS[args.workload]
     p = dlp.Problem(w["n"], w["degree"], w["batches"], w["seed"])
+    if args.batches > 0:  # bounded sample: the first --batches batches of the workload
+        p.batches = p.batches[:args.batches]
     nb = len(p.batches)
     sess = dlp.Session.from_problem(p, device=local_rank, narrow_lanes=args.lanes, blocks_per_sm=args.blocks_per_sm)
     dev_batches = [DeviceBatch(bt) for bt in p.batches]
@@ -331,7 +336,7 @@ def gpu_arm(args, td, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic (reference generator decisions, seed 42), inputs resident in HBM",
-        "config": {"workload": workload_desc(args.workload), "semantics": "ref", "parallelism": "replicas",
+        "config": {"workload": workload_desc(args.workload, args.batches), "semantics": "ref", "parallelism": "replicas",
                    "l2": "flushed before every step (512 MiB memset)", "narrow_lanes": args.lanes or 8,
                    "blocks_per_sm": args.blocks_per_sm or "occupancy",
                    "affected_edges_per_step": edges // max(args.steps, 1)},
@@ -500,6 +505,7 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2")
     ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--batches", type=int, default=0, help="replay only the first N batches (0: all)")
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--ref-budget-s", type=float, default=20.0)
