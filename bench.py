@@ -322,7 +322,8 @@ def gpu_arm(args, td, rank, world, local_rank):
     kern_s = sum(s["device_ms"] for s in stats0) / 1e3
     achieved = bytes_step / kern_s / 1e9 if kern_s > 0 else 0.0
     traffic = None
-    tf = ROOT / "profiles" / "traffic_engine_kernel_config2.json"
+    # DRAM traffic comes from an ncu capture of the same workload, when one exists
+    tf = ROOT / "profiles" / f"traffic_engine_kernel_{args.workload}.json"
     if tf.exists():
         try:
             traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
