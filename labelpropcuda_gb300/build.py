@@ -29,7 +29,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-std=c++17", "-lineinfo", "-fmad=false",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
     f"-I{INCLUDE}", f"-I{CSRC}",
-]
+] + os.environ.get("DLP_NVCC_EXTRA", "").split()  # e.g. -DDLP_SOLO_LANES=8 (build-time tuning)
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-I/usr/local/cuda/include",
              f"-I{INCLUDE}", f"-I{CSRC}"]
 

@@ -381,6 +381,7 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
   args.pass_budget = opts.pass_budget;
   args.slice_ns = opts.slice_ns;
   args.tag = e->steps + 1;
+  args.delta = e->cfg.delta;
   args.progress = sliced ? e->progress_dev : nullptr;
   DLP_CUDA_TRY(cudaEventRecord(e->ev[slot][0], e->stream));
   void *kargs[] = {&args};

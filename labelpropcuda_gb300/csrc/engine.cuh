@@ -63,6 +63,7 @@ struct EngineArgs {
   int pass_budget;                // propagation passes this launch runs at most (0: no limit)
   unsigned long long slice_ns;    // propagation time after which the launch stops (0: no limit)
   int tag;                        // unique per launch (stop requests)
+  float delta;                    // convergence threshold (the engine's, the same for every graph)
   int2 *progress;                 // per graph: {1 batch finished / 0 continues, passes so far}
 };
 

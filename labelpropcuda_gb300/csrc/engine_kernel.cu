@@ -910,17 +910,26 @@ __device__ __forceinline__ unsigned long long stop_code(const EngineArgs &e, int
 // during the stint, so loading them once is exact; every label written goes
 // back to HBM when the stint ends. Passes and arithmetic are those of the
 // grid path (same slot order in every row, same summation tree).
-constexpr int kVT = 2048;          // vertex-table slots (power of two), at most half in use
-constexpr int kVTUse = kVT / 2;
+constexpr int kVT = 2048;          // vertex-table slots (power of two), at most three quarters in use
+#ifndef DLP_SOLO_VT_USE
+#define DLP_SOLO_VT_USE (3 * kVT / 4)
+#endif
+constexpr int kVTUse = DLP_SOLO_VT_USE;  // slots in use at most (linear probing stays short below this)
 constexpr int kRP = 4096;          // row-pool entries
-constexpr int kSoloList = 1024;    // frontier capacity (vertex-table slots)
+// frontier capacity: a list holds distinct vertex-table slots, so it can never
+// need more entries than the table has slots in use
+constexpr int kSoloList = kVTUse;
+static_assert(kSoloList >= kVTUse, "a one-block frontier list must hold every slot in use");
 constexpr int kSoloEntry = 512;    // enter when the total frontier is at most this
 constexpr int kSoloMaxPasses = 65000;  // per stint, so that per-slot visit counts fit 16 bits
 constexpr unsigned long long kSoloBudgetNs = 100000000ull;
 constexpr unsigned long long kEmptyKey = ~0ull;
 constexpr unsigned char kWideLen = 255;
 constexpr unsigned short kNoRow = 0xffff;
-constexpr int kSoloG = 4;          // lanes per row in the one-block passes
+#ifndef DLP_SOLO_LANES
+#define DLP_SOLO_LANES 4
+#endif
+constexpr int kSoloG = DLP_SOLO_LANES;  // lanes per row in the one-block passes (build-time choice)
 
 struct SoloCache {
   unsigned long long key[kVT];   // (graph << 32) | vertex, kEmptyKey = free
@@ -934,7 +943,7 @@ struct SoloCache {
   unsigned char len[kVT];        // live row length, kWideLen when longer than 32
   signed char gt[kVT];
   unsigned char flags[kVT];      // bit0 written, bit1 in a frontier, bit2 buffer read at stint pass 0
-  int lastpass[kMaxGraphs];      // last pass each graph took part in during the stint
+  int lastpass[kMaxGraphs];      // last launch pass each graph took part in during the stint
   // Per list, indexed by stint pass % 3: the list read by pass j is filled
   // during pass j - 1 and its counters are cleared during pass j + 1, so a
   // thread reading them at the top of pass j never races a writer.
@@ -955,7 +964,7 @@ __device__ __forceinline__ unsigned mix64(unsigned long long x) {
 }
 
 // Slot of (g, v) in the vertex table, inserting (and loading from HBM) when
-// absent. The caller keeps the table at most half full.
+// absent. The caller keeps the table at most three quarters full.
 __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g, int v) {
   const unsigned long long key = (static_cast<unsigned long long>(g) << 32) | static_cast<unsigned>(v);
   unsigned h = mix64(key) & (kVT - 1);
@@ -979,7 +988,7 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
     if (prev == key) return static_cast<int>(h);
     h = (h + 1) & (kVT - 1);
   }
-  return -1;  // not reached: the table is never more than half full
+  return -1;  // not reached: the table always has free slots
 }
 
 template <int G>
@@ -1138,17 +1147,21 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
       }
       int changed = 0;
       if (valid && gl == 0) {
+        // nothing here reads the graph's record in global memory: delta is
+        // the engine's, and the pass offset is added at hand-back
         const int g = c.graph[su];
-        const GraphRec &r = e.recs[g];
         const float old = c.lab[src][su];
         const float nl = updated_label(tw, tl, old);
         c.lab[src ^ 1][su] = nl;
         c.flags[su] |= 3;
-        changed = fabsf(nl - old) > r.ba.delta;
+        changed = fabsf(nl - old) > e.delta;
         ++c.visits[su];  // a slot is in a list at most once
-        const int kg = k + r.ba.pass0;
-        c.lastpass[g] = kg;
-        if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
+        c.lastpass[g] = k;
+        if (rec_any) {
+          const GraphRec &r = e.recs[g];
+          const int kg = k + r.ba.pass0;
+          if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
+        }
       }
       changed = __shfl_sync(0xffffffffu, changed, 0, G);
       // changed vertex: non-deleted, non-GT neighbours and itself
@@ -1224,7 +1237,7 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   for (int g = tid; g < ng; g += kBlock) {
     BatchCounters *bc = e.recs[g].st.bc;
     const int kg = k + e.recs[g].ba.pass0;
-    if (c.lastpass[g] >= 0) bc->passes = c.lastpass[g] + 1;
+    if (c.lastpass[g] >= 0) bc->passes = c.lastpass[g] + e.recs[g].ba.pass0 + 1;
     bc->front_count[kg % 3][0] = bc->front_count[kg % 3][1] = 0;
     bc->front_count[(kg + 1) % 3][0] = bc->front_count[(kg + 1) % 3][1] = 0;
   }
@@ -1353,7 +1366,7 @@ constexpr int kSubEntry = 2048;   // enter when the total frontier is at most th
 constexpr int kSubLive = 4096;    // leave when it grows above this
 
 template <int G>
-__device__ bool sub_passes(const EngineArgs &e, int k0, int slot, int *pref, int *pref2) {
+__device__ bool sub_passes(const EngineArgs &e, int k0, int slot, int solo_from, int *pref, int *pref2) {
   const int lane = threadIdx.x & 31;
   const int warp0 = blockIdx.x * (kBlock / 32), nwarps = kSubBlocks * (kBlock / 32);
   const int t0 = blockIdx.x * kBlock + threadIdx.x, nthreads = kSubBlocks * kBlock;
@@ -1364,6 +1377,9 @@ __device__ bool sub_passes(const EngineArgs &e, int k0, int slot, int *pref, int
     pass_sizes(e, k, pref, pref2, tn, tw);
     const bool stop = ld_relaxed_u64(&e.ectl->sub_stop) == stop_code(e, k);
     if (tn + tw == 0 || tn + tw > kSubLive || stop || (e.pass_budget > 0 && k >= e.pass_budget)) break;
+    // a frontier the one-block mode can take goes back to it (cheaper passes),
+    // unless that mode recently could not hold its working set
+    if (k > k0 && (e.solo & 1) && tn + tw <= kSoloEntry && k >= solo_from) break;
     run_pass<G>(e, k, pref, tn, pref2, tw, lane, warp0 + (threadIdx.x >> 5), nwarps, t0, nthreads);
     if (t0 == 0 && ((k - k0) & 31) == 31 && global_timer_ns() - start > 100000000ull)
       e.ectl->sub_stop = stop_code(e, k + 1);
@@ -1385,6 +1401,7 @@ __device__ bool sub_passes(const EngineArgs &e, int k0, int slot, int *pref, int
 template <int G>
 __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2, SoloCache &solo, int &k_end) {
   int no_small_at = -1;  // a pass the small modes declined goes to the full grid
+  int solo_from = 0;     // the one-block mode declined: not tried again before this pass
   int stint = 0;
   int k = 0;
   for (;; ++k) {
@@ -1394,20 +1411,21 @@ __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2
     if (e.pass_budget > 0 && k >= e.pass_budget) break;
     if (ld_relaxed_u64(&e.ectl->slice_stop) == stop_code(e, k)) break;
     if (c.gtid == 0) e.ectl->where_pass = k;
-    const bool solo_ok = (e.solo & 1) && tn + tw <= kSoloEntry && k != no_small_at;
+    const bool solo_ok = (e.solo & 1) && tn + tw <= kSoloEntry && k != no_small_at && k >= solo_from;
     const bool sub_ok = !solo_ok && (e.solo & 2) && gridDim.x > 2 * kSubBlocks && tn + tw <= kSubEntry &&
                         k != no_small_at;
     if (solo_ok || sub_ok) {
       if (solo_ok) {
         if (blockIdx.x == 0) solo_passes<kSoloG>(e, k, stint & 1, solo);
       } else if (blockIdx.x < kSubBlocks) {
-        if (!sub_passes<G>(e, k, stint & 1, pref, pref2)) return false;
+        if (!sub_passes<G>(e, k, stint & 1, solo_from, pref, pref2)) return false;
       }
       if (!grid_sync(&e.ectl->bar, &e.ectl->err, e.timeout_ns)) return false;
       const int done = ld_relaxed_i32(&e.ectl->solo_passes[stint & 1]);
       const int kk = ld_relaxed_i32(&e.ectl->solo_k[stint & 1]);
       ++stint;
       if (done == 0) no_small_at = k;
+      if (solo_ok && done == 0) solo_from = k + 256;
       k = kk - 1;  // the loop increment resumes at pass kk
       continue;
     }
