@@ -991,6 +991,118 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
   return -1;  // not reached: the table always has free slots
 }
 
+// One pass of the one-block mode over the rows of `cur` (cnt entries), G lanes
+// per row: every row from shared memory, marks into `next` and the counters of
+// list nq. G only sets how the rows are spread over the block's threads; the
+// arithmetic and the marked set do not depend on it.
+template <int G>
+__device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, const unsigned short *cur,
+                                          unsigned short *next, int cnt, int nq, int k, bool rec_any) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kWarps = kBlock / 32;
+  constexpr int R = 32 / G;
+  constexpr int GPW = 32 / G;
+  const int grp = lane / G, gl = lane & (G - 1);
+
+  for (int base = warp * GPW; base < cnt; base += kWarps * GPW) {
+    const int item = base + grp;
+    const bool valid = item < cnt;
+    const int su = valid ? cur[item] : 0;
+    const int len = valid ? c.len[su] : 0;
+    const int off = valid ? c.row[su] : 0;
+    const int src = valid ? (((c.flags[su] >> 2) ^ k) & 1) : 0;
+    float sw[R], sl[R];
+    int vv[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int ee = gl + G * r;
+      sw[r] = 0.0f;
+      sl[r] = 0.0f;
+      vv[r] = -1;
+      if (ee < len) {
+        const int2 ent = c.rp[off + ee];
+        vv[r] = ent.x;
+        if (ent.x >= 0) {
+          const float wt = __int_as_float(ent.y);
+          sw[r] = wt;
+          sl[r] = __fmaf_rn(wt, c.lab[src][ent.x], 0.0f);
+        }
+      }
+    }
+#pragma unroll
+    for (int half = R / 2; half >= 1; half >>= 1)
+#pragma unroll
+      for (int r = 0; r < half; ++r) {
+        sw[r] = sw[r] + sw[r + half];
+        sl[r] = sl[r] + sl[r + half];
+      }
+    float tw = sw[0], tl = sl[0];
+#pragma unroll
+    for (int o = G / 2; o >= 1; o >>= 1) {
+      tw = tw + __shfl_down_sync(0xffffffffu, tw, o, G);
+      tl = tl + __shfl_down_sync(0xffffffffu, tl, o, G);
+    }
+    int changed = 0;
+    if (valid && gl == 0) {
+      // nothing here reads the graph's record in global memory: delta is
+      // the engine's, and the pass offset is added at hand-back
+      const int g = c.graph[su];
+      const float old = c.lab[src][su];
+      const float nl = updated_label(tw, tl, old);
+      c.lab[src ^ 1][su] = nl;
+      c.flags[su] |= 3;
+      changed = fabsf(nl - old) > e.delta;
+      ++c.visits[su];  // a slot is in a list at most once
+      c.lastpass[g] = k;
+      if (rec_any) {
+        const GraphRec &r = e.recs[g];
+        const int kg = k + r.ba.pass0;
+        if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
+      }
+    }
+    changed = __shfl_sync(0xffffffffu, changed, 0, G);
+    // changed vertex: non-deleted, non-GT neighbours and itself
+    // (src/iterativePropagation.cu:200-216). All marks first, then one
+    // reservation in the next list for the whole warp.
+    unsigned fresh = 0;
+    if (changed) {
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r) {
+        const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
+        if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
+      }
+    }
+    const int nf = __popc(fresh);
+    int add = 0, wide = 0;
+#pragma unroll
+    for (int r = 0; r < R + 1; ++r)
+      if ((fresh >> r) & 1u) {
+        const int ns = r < R ? vv[r] : su;
+        const int l = c.len[ns];
+        if (l == kWideLen) wide = 1;
+        else if (c.row[ns] == kNoRow) add += l;
+      }
+    int incl = nf;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int tot = __shfl_sync(0xffffffffu, incl, 31);
+    add = __reduce_add_sync(0xffffffffu, add);
+    wide = __reduce_or_sync(0xffffffffu, wide);
+    int at = 0;
+    if (lane == 31 && tot) {
+      at = atomicAdd(&c.cnt[nq], tot);
+      if (add) atomicAdd(&c.need[nq], add);
+      if (wide) c.wide[nq] = 1;
+    }
+    at = __shfl_sync(0xffffffffu, at, 31) + incl - nf;
+#pragma unroll
+    for (int r = 0; r < R + 1; ++r)
+      if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
+  }
+}
 template <int G>
 __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c) {
   const int ng = e.ng;
@@ -1104,107 +1216,12 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
         const int kg = k + 1 + r.ba.pass0;
         if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
       }
-    // the pass: every frontier row from shared memory
+    // the pass: every frontier row from shared memory; a frontier larger
+    // than one round of 4-lane groups takes 2-lane groups (one round up to 256)
     const unsigned short *cur = c.list[p];
     unsigned short *next = c.list[p ^ 1];
-    for (int base = warp * GPW; base < cnt; base += kWarps * GPW) {
-      const int item = base + grp;
-      const bool valid = item < cnt;
-      const int su = valid ? cur[item] : 0;
-      const int len = valid ? c.len[su] : 0;
-      const int off = valid ? c.row[su] : 0;
-      const int src = valid ? (((c.flags[su] >> 2) ^ k) & 1) : 0;
-      float sw[R], sl[R];
-      int vv[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int ee = gl + G * r;
-        sw[r] = 0.0f;
-        sl[r] = 0.0f;
-        vv[r] = -1;
-        if (ee < len) {
-          const int2 ent = c.rp[off + ee];
-          vv[r] = ent.x;
-          if (ent.x >= 0) {
-            const float wt = __int_as_float(ent.y);
-            sw[r] = wt;
-            sl[r] = __fmaf_rn(wt, c.lab[src][ent.x], 0.0f);
-          }
-        }
-      }
-#pragma unroll
-      for (int half = R / 2; half >= 1; half >>= 1)
-#pragma unroll
-        for (int r = 0; r < half; ++r) {
-          sw[r] = sw[r] + sw[r + half];
-          sl[r] = sl[r] + sl[r + half];
-        }
-      float tw = sw[0], tl = sl[0];
-#pragma unroll
-      for (int o = G / 2; o >= 1; o >>= 1) {
-        tw = tw + __shfl_down_sync(0xffffffffu, tw, o, G);
-        tl = tl + __shfl_down_sync(0xffffffffu, tl, o, G);
-      }
-      int changed = 0;
-      if (valid && gl == 0) {
-        // nothing here reads the graph's record in global memory: delta is
-        // the engine's, and the pass offset is added at hand-back
-        const int g = c.graph[su];
-        const float old = c.lab[src][su];
-        const float nl = updated_label(tw, tl, old);
-        c.lab[src ^ 1][su] = nl;
-        c.flags[su] |= 3;
-        changed = fabsf(nl - old) > e.delta;
-        ++c.visits[su];  // a slot is in a list at most once
-        c.lastpass[g] = k;
-        if (rec_any) {
-          const GraphRec &r = e.recs[g];
-          const int kg = k + r.ba.pass0;
-          if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
-        }
-      }
-      changed = __shfl_sync(0xffffffffu, changed, 0, G);
-      // changed vertex: non-deleted, non-GT neighbours and itself
-      // (src/iterativePropagation.cu:200-216). All marks first, then one
-      // reservation in the next list for the whole warp.
-      unsigned fresh = 0;
-      if (changed) {
-#pragma unroll
-        for (int r = 0; r < R + 1; ++r) {
-          const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
-          if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
-        }
-      }
-      const int nf = __popc(fresh);
-      int add = 0, wide = 0;
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r)
-        if ((fresh >> r) & 1u) {
-          const int ns = r < R ? vv[r] : su;
-          const int l = c.len[ns];
-          if (l == kWideLen) wide = 1;
-          else if (c.row[ns] == kNoRow) add += l;
-        }
-      int incl = nf;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const int tot = __shfl_sync(0xffffffffu, incl, 31);
-      add = __reduce_add_sync(0xffffffffu, add);
-      wide = __reduce_or_sync(0xffffffffu, wide);
-      int at = 0;
-      if (lane == 31 && tot) {
-        at = atomicAdd(&c.cnt[nq], tot);
-        if (add) atomicAdd(&c.need[nq], add);
-        if (wide) c.wide[nq] = 1;
-      }
-      at = __shfl_sync(0xffffffffu, at, 31) + incl - nf;
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r)
-        if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
-    }
+    if (cnt > kBlock / G) solo_rows<2>(e, c, cur, next, cnt, nq, k, rec_any);
+    else solo_rows<G>(e, c, cur, next, cnt, nq, k, rec_any);
     // time budgets: checked by thread 0, they stop the stint two passes on
     // (a thread still at the top of this pass must not see the request)
     if (tid == 0 && (j & 15) == 15) {
