@@ -1216,12 +1216,14 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
         const int kg = k + 1 + r.ba.pass0;
         if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
       }
-    // the pass: every frontier row from shared memory; a frontier larger
-    // than one round of 4-lane groups takes 2-lane groups (one round up to 256)
+    // the pass: every frontier row from shared memory, with the widest lane
+    // groups that still take the whole frontier in one round of the block
+    // (8 lanes up to 64 rows, 4 up to 128, else 2)
     const unsigned short *cur = c.list[p];
     unsigned short *next = c.list[p ^ 1];
-    if (cnt > kBlock / G) solo_rows<2>(e, c, cur, next, cnt, nq, k, rec_any);
-    else solo_rows<G>(e, c, cur, next, cnt, nq, k, rec_any);
+    if (cnt <= kBlock / 8) solo_rows<8>(e, c, cur, next, cnt, nq, k, rec_any);
+    else if (cnt <= kBlock / 4) solo_rows<4>(e, c, cur, next, cnt, nq, k, rec_any);
+    else solo_rows<2>(e, c, cur, next, cnt, nq, k, rec_any);
     // time budgets: checked by thread 0, they stop the stint two passes on
     // (a thread still at the top of this pass must not see the request)
     if (tid == 0 && (j & 15) == 15) {
