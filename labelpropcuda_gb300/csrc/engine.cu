@@ -74,7 +74,7 @@ int dalloc(T **p, size_t count, std::vector<void *> &owned, size_t &counted, std
 // Device bytes a resident graph needs (fixed part).
 size_t graph_bytes(int64_t n, int64_t m, bool truth, bool bmap, bool record) {
   size_t b = 4 * (n + 1) + 16 * m + 4 * n + 2 * n + 4 * n + 8 * n + 4 * n + 16 * n + 4 * n * 2 + 4 * n * 5 +
-             4 * n + 16 * n + sizeof(dlp_batch_stats) * kStepRing;
+             4 * n + 16 * n + n + sizeof(dlp_batch_stats) * kStepRing;
   if (truth) b += n;
   if (bmap) b += 4 * n;
   if (record) b += 4 * n * 4 + 4 * dlp::session::kRecordIters;
@@ -238,6 +238,7 @@ int reset_graph(dlp_engine *e, GraphSlot *g, int gid) {
   DLP_CUDA_TRY(cudaMemsetAsync(d.act_len, 0, sizeof(int) * n, q));
   DLP_CUDA_TRY(cudaMemsetAsync(d.status, dlp::kDeleted, n, q));
   DLP_CUDA_TRY(cudaMemsetAsync(d.gt, 0xff, n, q));
+  DLP_CUDA_TRY(cudaMemsetAsync(d.nmeta, 1, n, q));  // no ground truth, empty rows
   DLP_CUDA_TRY(cudaMemsetAsync(d.contrib, 0xff, sizeof(int) * n, q));
   DLP_CUDA_TRY(cudaMemsetAsync(d.local, 0xff, sizeof(int) * n, q));
   for (unsigned *p : {d.del_stamp, d.gt_stamp, d.dirty_stamp, d.front_stamp})
@@ -515,6 +516,7 @@ int alloc_graph(dlp_engine *e, int n, int64_t m, bool with_truth, bool with_bmap
       (st = dalloc(&d.flist, 3 * static_cast<size_t>(n), o, b, z)) ||
       (st = dalloc(&d.touched, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&d.par, n, o, b, z)) ||
       (st = dalloc(&d.acc, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&g->stats, kStepRing, o, b, z)) ||
+      (st = dalloc(&d.nmeta, n, o, b, z)) ||
       (with_truth && (st = dalloc(&truth, n, o, b, z))) || (with_bmap && (st = dalloc(&bmap, n, o, b, z))) ||
       (e->cfg.record &&
        ((st = dalloc(&d.rec_front0, n, o, b, z)) || (st = dalloc(&d.rec_root, n, o, b, z)) ||

@@ -317,6 +317,7 @@ __device__ void phase_b(const EngineArgs &e, const Ctx &c, int *pref) {
     const int v = a.gt_ids[i];
     const float l = a.gt_lab[i];
     s.gt[v] = l < 0.5f ? 0 : 1;
+    s.nmeta[v] = s.act_len[v] > kNarrowMax ? 2 : 0;  // not markable any more
     s.lab0[v] = l;
     s.lab1[v] = l;
     if (!(a.spec && s.del_stamp[v] == w.cur)) s.status[v] = kGroundTruth;
@@ -396,7 +397,11 @@ __device__ void phase_c(const EngineArgs &e, const Ctx &c, int *pref) {
       seed_mark(w, keep && del_row, ent.x);
       pos += __popc(m);
     }
-    if (valid && gl == 0) s.act_len[u] = keep_row ? pos : 0;
+    if (valid && gl == 0) {
+      const int len = keep_row ? pos : 0;
+      s.act_len[u] = len;
+      s.nmeta[u] = static_cast<uint8_t>((s.gt[u] < 0 ? 1 : 0) | (len > kNarrowMax ? 2 : 0));
+    }
   });
 
   // spec: neighbours of every deleted vertex that was live before this batch's
@@ -733,8 +738,9 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
         const float wt = __int_as_float(ent.y);
         sw[r] = wt;                               // 0 + w
         sl[r] = __fmaf_rn(wt, src[ent.x], 0.0f);  // fma(w, F_v, 0)
-        if (s.gt[ent.x] < 0) vv[r] = ent.x;
-        if (s.act_len[ent.x] > kNarrowMax) wb |= 1u << r;
+        const unsigned meta = s.nmeta[ent.x];
+        if (meta & 1u) vv[r] = ent.x;
+        if (meta & 2u) wb |= 1u << r;
       }
     }
   }

@@ -63,6 +63,8 @@ struct DevState {
   int *act_len;             // live row length
   int8_t *status;           // host-side status (src/dynLP.cu:117-130)
   int8_t *gt;               // -1 / 0 / 1
+  uint8_t *nmeta;           // what propagation needs about a neighbour, in one byte:
+                            // bit 0 markable (no ground truth), bit 1 live row longer than 32
   const uint8_t *truth;     // 0 / 1
   int *contrib;             // accuracy contribution: -1 none, 0 wrong, 1 right
   const int *batch_map;     // arrival batch per vertex, or null
