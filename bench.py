@@ -312,6 +312,9 @@ def gpu_arm(args, td, rank, world, local_rank):
         e2e_s += time.perf_counter() - t0
     e2e_max = dist_max(td, e2e_s)
     e2e_value = dist_sum(td, e2e_edges) / e2e_max if e2e_max > 0 else 0.0
+    # every rank serves its shard of the mixed stream (the aggregation inside
+    # is collective, so it runs before the other ranks leave)
+    served = None if args.no_served else served_block(args, local_rank, rank, world, td)
 
     if rank != 0:
         return 0
@@ -331,7 +334,6 @@ def gpu_arm(args, td, rank, world, local_rank):
             traffic = None
     # CPU baseline: the oracle, single thread, bounded sample of the same workload
     cpu_edges, cpu_t, cpu_done = cpu_run(p, 1, args.cpu_budget_s)
-    served = None if args.no_served or world > 1 else served_block(args, local_rank)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
@@ -372,6 +374,22 @@ def mix_sizes(count: int, lo: float, hi: float, seed: int):
     return [(int(n[i]), (3, 5, 7)[i % 3], 10, i) for i in range(count)]
 
 
+def shard_graphs(specs, rank: int, world: int) -> list[int]:
+    """Indices of the graphs rank `rank` of `world` serves: graphs are
+    independent, so they are split across GPUs with no collective on the data
+    path. Greedy by expected edges (n x degree), largest first, to the least
+    loaded rank; ties go to the lower rank, so every rank computes the same
+    split."""
+    load = [0] * world
+    mine = []
+    for i in sorted(range(len(specs)), key=lambda i: (-specs[i][0] * specs[i][1], i)):
+        r = min(range(world), key=lambda r: (load[r], r))
+        load[r] += specs[i][0] * specs[i][1]
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
+
+
 def make_problems(specs, threads: int):
     import concurrent.futures as cf
     import labelpropcuda_gb300 as dlp
@@ -379,18 +397,21 @@ def make_problems(specs, threads: int):
         return list(ex.map(lambda s: dlp.Problem(*s), specs))
 
 
-def served_block(args, local_rank) -> dict:
+def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     """The mixed-graph stream: N resident graphs, every graph's 10 batches.
     batched = one engine step per batch index over all graphs (one launch per
     step, per-graph convergence); served = the continuous-batching server
     replaying the requests (all queued at once = saturation, then Poisson at
     half that request rate); plain = the same server in serial mode (one
-    request at a time, run to its end), on a bounded sample of the trace."""
+    request at a time, run to its end), on a bounded sample of the trace.
+    With several ranks each serves its shard of the graphs (shard_graphs);
+    rates are summed over ranks and times take the slowest rank."""
     import numpy as np
     import labelpropcuda_gb300 as dlp
     from labelpropcuda_gb300 import PackedBatches
     t_setup = time.perf_counter()
-    specs = mix_sizes(args.served_graphs, 1e3, 5e5, 1000003)
+    all_specs = mix_sizes(args.served_graphs, 1e3, 5e5, 1000003)
+    specs = [all_specs[i] for i in shard_graphs(all_specs, rank, world)]
     probs = make_problems(specs, min(16, os.cpu_count() or 1))
     lanes, bps, tune = args.served_lanes, 0, None
     if lanes == 0:  # autotune the launch shape on a sample of the same size distribution
@@ -422,7 +443,9 @@ def served_block(args, local_rank) -> dict:
         ae = sum(eng.stats(g, b)["affected_edges"] for g in gids for b in range(nb))
         return ms, ae
     b_ms, b_ae = batched_run()
-    batched = {"value": b_ae / (sum(b_ms) / 1e3), "ms_per_step": sum(b_ms) / nb,
+    b_t = dist_max(td, sum(b_ms) / 1e3)
+    b_ae = int(dist_sum(td, b_ae))
+    batched = {"value": b_ae / b_t, "ms_per_step": 1e3 * b_t / nb,
                "step_ms_p50": percentile(b_ms, 0.5), "step_ms_max": max(b_ms),
                "affected_edges": b_ae, "launches": 2 * nb,
                "timing": "CUDA events around each step, batches resident in HBM"}
@@ -443,12 +466,13 @@ def served_block(args, local_rank) -> dict:
 
     # saturation: everything queued at t = 0
     res, span = replay(reqs)
-    sat_ae = sum(r["stats"]["affected_edges"] for r in res)
-    sat_rate = len(res) / span
+    sat_ae = dist_sum(td, sum(r["stats"]["affected_edges"] for r in res))
+    sat_rate = len(res) / span  # this rank's, for its own Poisson trace
+    span = dist_max(td, span)
     svc = [1e3 * (r["finish_s"] - r["admit_s"]) for r in res]
-    served_sat = {"value": sat_ae / span, "makespan_s": span, "requests": len(res),
-                  "requests_per_s": sat_rate, "service_ms_p50": percentile(svc, 0.5),
-                  "service_ms_p99": percentile(svc, 0.99)}
+    served_sat = {"value": sat_ae / span, "makespan_s": span, "requests": int(dist_sum(td, len(res))),
+                  "requests_per_s": dist_sum(td, sat_rate), "service_ms_p50": dist_max(td, percentile(svc, 0.5)),
+                  "service_ms_p99": dist_max(td, percentile(svc, 0.99))}
     # Poisson arrivals at half the saturated request rate (each graph's
     # batches keep their order: arrival k goes to the next request in the list)
     rng = np.random.default_rng(7)
@@ -458,10 +482,11 @@ def served_block(args, local_rank) -> dict:
     res, span = replay(trace)
     srv.close()
     lat = [1e3 * (r["finish_s"] - r["arrival_s"]) for r in res]
-    p_ae = sum(r["stats"]["affected_edges"] for r in res)
-    served_poisson = {"offered_requests_per_s": rate, "value": p_ae / span, "makespan_s": span,
-                      "latency_ms_p50": percentile(lat, 0.5), "latency_ms_p99": percentile(lat, 0.99),
-                      "latency_ms_max": max(lat)}
+    p_ae = dist_sum(td, sum(r["stats"]["affected_edges"] for r in res))
+    span = dist_max(td, span)
+    served_poisson = {"offered_requests_per_s": dist_sum(td, rate), "value": p_ae / span, "makespan_s": span,
+                      "latency_ms_p50": dist_max(td, percentile(lat, 0.5)),
+                      "latency_ms_p99": dist_max(td, percentile(lat, 0.99)), "latency_ms_max": dist_max(td, max(lat))}
     # plain: serial, bounded sample — whole graphs (all 10 batches each, in
     # order) taken in a seeded random order until the time budget is used
     reset_all()
@@ -479,12 +504,13 @@ def served_block(args, local_rank) -> dict:
         pl_svc += [1e3 * (r["finish_s"] - r["admit_s"]) for r in res]
         graphs_done += 1
     srv.close()
-    plain_v = pl_ae / pl_t if pl_t > 0 else 0.0
+    plain_v = dist_sum(td, pl_ae / pl_t if pl_t > 0 else 0.0)  # every GPU runs its own plain path
     plain = {"value": plain_v, "requests": graphs_done * nb, "seconds": pl_t,
              "service_ms_p50": percentile(pl_svc, 0.5), "service_ms_p99": percentile(pl_svc, 0.99),
              "sample": f"{graphs_done} of {len(gids)} graphs (seeded random order), all {nb} batches each, "
                        f"one request at a time"}
-    out = {"workload": (f"mixed-graph stream: {len(probs)} graphs, n log-uniform on [1e3, 5e5] (numpy seed "
+    out = {"workload": (f"mixed-graph stream: {len(all_specs)} graphs ({len(probs)} on this rank of {world}), "
+                        f"n log-uniform on [1e3, 5e5] (numpy seed "
                         f"1000003), degree {{3,5,7}}[i mod 3], generator seed i, 10 batches each (90/1/9), "
                         f"delta 1e-4, maxIter 1e5, ref semantics; {vertices} vertices, {edges_full} directed "
                         f"edges in all"),
