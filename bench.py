@@ -397,6 +397,11 @@ def make_problems(specs, threads: int):
         return list(ex.map(lambda s: dlp.Problem(*s), specs))
 
 
+def progress(msg: str) -> None:
+    """Progress of a long run on stderr (stdout carries only the JSON line)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     """The mixed-graph stream: N resident graphs, every graph's 10 batches.
     batched = one engine step per batch index over all graphs (one launch per
@@ -410,7 +415,13 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     import labelpropcuda_gb300 as dlp
     from labelpropcuda_gb300 import PackedBatches
     t_setup = time.perf_counter()
-    all_specs = mix_sizes(args.served_graphs, 1e3, 5e5, 1000003)
+    if args.served_shape == "stream":
+        # serving-stream shape: larger graphs, requests of about 2% of a graph
+        # (40 batches per graph), the first --served-batches requests of each
+        lo, hi, count, gen_batches, nb = 1e4, 5e6, args.served_graphs, 40, args.served_batches
+    else:
+        lo, hi, count, gen_batches, nb = 1e3, 5e5, args.served_graphs, 10, 10
+    all_specs = [(n, d, gen_batches, sd) for n, d, _, sd in mix_sizes(count, lo, hi, 1000003)]
     specs = [all_specs[i] for i in shard_graphs(all_specs, rank, world)]
     probs = make_problems(specs, min(16, os.cpu_count() or 1))
     lanes, bps, tune = args.served_lanes, 0, None
@@ -420,11 +431,13 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
         lanes, bps = tune["narrow_lanes"], tune["blocks_per_sm"]
     eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=lanes, blocks_per_sm=bps)
     gids = [eng.add_problem(p) for p in probs]
-    nb = 10
+    for p in probs:  # the requests of this run: each graph's first nb batches
+        p.batches = p.batches[:nb]
     for g, p in zip(gids, probs):  # scratch sized up front: no allocation inside the timed runs
         eng.reserve(g, max(bt.edge_src.size for bt in p.batches), max(bt.deleted.size for bt in p.batches))
     packed = [PackedBatches([p.batches[b] for p in probs]) for b in range(nb)]
     setup_s = time.perf_counter() - t_setup
+    progress(f"served setup {setup_s:.1f} s: {len(probs)} graphs, lanes {lanes}, blocks/SM {bps or 'occupancy'}")
     vertices = sum(p.num_nodes for p in probs)
     edges_full = sum(p.num_edges for p in probs)
 
@@ -449,6 +462,7 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
                "step_ms_p50": percentile(b_ms, 0.5), "step_ms_max": max(b_ms),
                "affected_edges": b_ae, "launches": 2 * nb,
                "timing": "CUDA events around each step, batches resident in HBM"}
+    progress(f"batched {batched['value'] / 1e9:.3f} G/s, step max {max(b_ms):.0f} ms")
 
     reqs = [(0.0, g, b, probs[i].batches[b]) for b in range(nb) for i, g in enumerate(gids)]
 
@@ -473,6 +487,7 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     served_sat = {"value": sat_ae / span, "makespan_s": span, "requests": int(dist_sum(td, len(res))),
                   "requests_per_s": dist_sum(td, sat_rate), "service_ms_p50": dist_max(td, percentile(svc, 0.5)),
                   "service_ms_p99": dist_max(td, percentile(svc, 0.99))}
+    progress(f"served saturated {served_sat['value'] / 1e9:.3f} G/s, makespan {span:.1f} s")
     # Poisson arrivals at half the saturated request rate (each graph's
     # batches keep their order: arrival k goes to the next request in the list)
     rng = np.random.default_rng(7)
@@ -487,6 +502,8 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     served_poisson = {"offered_requests_per_s": dist_sum(td, rate), "value": p_ae / span, "makespan_s": span,
                       "latency_ms_p50": dist_max(td, percentile(lat, 0.5)),
                       "latency_ms_p99": dist_max(td, percentile(lat, 0.99)), "latency_ms_max": dist_max(td, max(lat))}
+    progress(f"served poisson {served_poisson['value'] / 1e9:.3f} G/s, p50 {served_poisson['latency_ms_p50']:.1f} ms, "
+             f"p99 {served_poisson['latency_ms_p99']:.1f} ms")
     # plain: serial, bounded sample — whole graphs (all 10 batches each, in
     # order) taken in a seeded random order until the time budget is used
     reset_all()
@@ -505,13 +522,15 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
         graphs_done += 1
     srv.close()
     plain_v = dist_sum(td, pl_ae / pl_t if pl_t > 0 else 0.0)  # every GPU runs its own plain path
+    progress(f"plain {plain_v / 1e6:.1f} M/s over {graphs_done} graphs")
     plain = {"value": plain_v, "requests": graphs_done * nb, "seconds": pl_t,
              "service_ms_p50": percentile(pl_svc, 0.5), "service_ms_p99": percentile(pl_svc, 0.99),
              "sample": f"{graphs_done} of {len(gids)} graphs (seeded random order), all {nb} batches each, "
                        f"one request at a time"}
-    out = {"workload": (f"mixed-graph stream: {len(all_specs)} graphs ({len(probs)} on this rank of {world}), "
-                        f"n log-uniform on [1e3, 5e5] (numpy seed "
-                        f"1000003), degree {{3,5,7}}[i mod 3], generator seed i, 10 batches each (90/1/9), "
+    out = {"workload": (f"mixed-graph stream ({args.served_shape}): {len(all_specs)} graphs ({len(probs)} on this "
+                        f"rank of {world}), n log-uniform on [{lo:.0e}, {hi:.0e}], {gen_batches} batches generated per "
+                        f"graph, the first {nb} served (numpy seed "
+                        f"1000003), degree {{3,5,7}}[i mod 3], generator seed i, batches 90/1/9 insert/GT/delete, "
                         f"delta 1e-4, maxIter 1e5, ref semantics; {vertices} vertices, {edges_full} directed "
                         f"edges in all"),
            "setup_s": setup_s, "batched": batched, "served_saturated": served_sat,
@@ -537,6 +556,10 @@ def main(argv=None) -> int:
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--ref-budget-s", type=float, default=20.0)
     ap.add_argument("--served-graphs", type=int, default=64)
+    ap.add_argument("--served-shape", choices=["mixed", "stream"], default="mixed",
+                    help="mixed: sizes 1e3-5e5, 10 batches; stream: sizes 1e4-5e6, 40 batches (about 2%% of a graph "
+                         "per request), the first --served-batches of each served")
+    ap.add_argument("--served-batches", type=int, default=5)
     ap.add_argument("--served-lanes", type=int, default=0, help="0: autotune")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--slice-us", type=float, default=1000.0)
