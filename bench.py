@@ -417,10 +417,13 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     t_setup = time.perf_counter()
     if args.served_shape == "stream":
         # serving-stream shape: larger graphs, requests of about 2% of a graph
-        # (40 batches per graph), the first --served-batches requests of each
+        # (40 batches per graph); every graph first takes its first `skip`
+        # batches (untimed), then --served-batches more are served
         lo, hi, count, gen_batches, nb = 1e4, 5e6, args.served_graphs, 40, args.served_batches
+        skip = 20 if args.served_skip < 0 else args.served_skip
     else:
         lo, hi, count, gen_batches, nb = 1e3, 5e5, args.served_graphs, 10, 10
+        skip = 0
     all_specs = [(n, d, gen_batches, sd) for n, d, _, sd in mix_sizes(count, lo, hi, 1000003)]
     specs = [all_specs[i] for i in shard_graphs(all_specs, rank, world)]
     probs = make_problems(specs, min(16, os.cpu_count() or 1))
@@ -431,10 +434,11 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
         lanes, bps = tune["narrow_lanes"], tune["blocks_per_sm"]
     eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=lanes, blocks_per_sm=bps)
     gids = [eng.add_problem(p) for p in probs]
-    for p in probs:  # the requests of this run: each graph's first nb batches
-        p.batches = p.batches[:nb]
-    for g, p in zip(gids, probs):  # scratch sized up front: no allocation inside the timed runs
-        eng.reserve(g, max(bt.edge_src.size for bt in p.batches), max(bt.deleted.size for bt in p.batches))
+    warm = [p.batches[:skip] for p in probs]  # applied untimed before every measured phase
+    for p in probs:  # the requests of this run: batches skip .. skip+nb-1 of each graph
+        p.batches = p.batches[skip:skip + nb]
+    for g, p, w in zip(gids, probs, warm):  # scratch sized up front: no allocation inside the timed runs
+        eng.reserve(g, max(bt.edge_src.size for bt in p.batches + w), max(bt.deleted.size for bt in p.batches + w))
     packed = [PackedBatches([p.batches[b] for p in probs]) for b in range(nb)]
     setup_s = time.perf_counter() - t_setup
     progress(f"served setup {setup_s:.1f} s: {len(probs)} graphs, lanes {lanes}, blocks/SM {bps or 'occupancy'}")
@@ -444,16 +448,19 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     def reset_all():
         for g in gids:
             eng.reset_graph(g)
+        for b in range(skip):  # the graphs' state before the served batches (untimed)
+            eng.step([(g, b, w[b]) for g, w in zip(gids, warm)], wait=False)
+        eng.synchronize()
 
     # batched: one launch per step over every graph
     def batched_run():
         reset_all()
         first = eng.steps
         for b in range(nb):
-            eng.step_device([(g, b, packed[b].view(i)) for i, g in enumerate(gids)])
+            eng.step_device([(g, skip + b, packed[b].view(i)) for i, g in enumerate(gids)])
         eng.synchronize()
         ms = [eng.elapsed_ms(first + b, first + b) for b in range(nb)]
-        ae = sum(eng.stats(g, b)["affected_edges"] for g in gids for b in range(nb))
+        ae = sum(eng.stats(g, skip + b)["affected_edges"] for g in gids for b in range(nb))
         return ms, ae
     b_ms, b_ae = batched_run()
     b_t = dist_max(td, sum(b_ms) / 1e3)
@@ -464,7 +471,7 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
                "timing": "CUDA events around each step, batches resident in HBM"}
     progress(f"batched {batched['value'] / 1e9:.3f} G/s, step max {max(b_ms):.0f} ms")
 
-    reqs = [(0.0, g, b, probs[i].batches[b]) for b in range(nb) for i, g in enumerate(gids)]
+    reqs = [(0.0, g, skip + b, probs[i].batches[b]) for b in range(nb) for i, g in enumerate(gids)]
 
     srv = dlp.Server(eng, memory_budget_bytes=150 << 30, slice_us=args.slice_us)
     for g, p in zip(gids, probs):
@@ -515,7 +522,7 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     for i in order:
         if pl_t >= args.plain_budget_s:
             break
-        res, span = srv.replay([(0.0, gids[i], b, probs[i].batches[b]) for b in range(nb)])
+        res, span = srv.replay([(0.0, gids[i], skip + b, probs[i].batches[b]) for b in range(nb)])
         pl_ae += sum(r["stats"]["affected_edges"] for r in res)
         pl_t += span
         pl_svc += [1e3 * (r["finish_s"] - r["admit_s"]) for r in res]
@@ -529,7 +536,7 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
                        f"one request at a time"}
     out = {"workload": (f"mixed-graph stream ({args.served_shape}): {len(all_specs)} graphs ({len(probs)} on this "
                         f"rank of {world}), n log-uniform on [{lo:.0e}, {hi:.0e}], {gen_batches} batches generated per "
-                        f"graph, the first {nb} served (numpy seed "
+                        f"graph, batches {skip}-{skip + nb - 1} served after the first {skip} (numpy seed "
                         f"1000003), degree {{3,5,7}}[i mod 3], generator seed i, batches 90/1/9 insert/GT/delete, "
                         f"delta 1e-4, maxIter 1e5, ref semantics; {vertices} vertices, {edges_full} directed "
                         f"edges in all"),
@@ -560,6 +567,8 @@ def main(argv=None) -> int:
                     help="mixed: sizes 1e3-5e5, 10 batches; stream: sizes 1e4-5e6, 40 batches (about 2%% of a graph "
                          "per request), the first --served-batches of each served")
     ap.add_argument("--served-batches", type=int, default=5)
+    ap.add_argument("--served-skip", type=int, default=-1, help="stream shape: batches applied before serving "
+                    "(default 20)")
     ap.add_argument("--served-lanes", type=int, default=0, help="0: autotune")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--slice-us", type=float, default=1000.0)
