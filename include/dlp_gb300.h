@@ -7,14 +7,19 @@
  * addresses on the current device; `stream` is a cudaStream_t passed as void*
  * (NULL = the legacy default stream).
  *
- * Three groups of entry points:
+ * Groups of entry points:
  *   1. input generation (host only),
  *   2. a resident session that keeps one dynamic graph on the GPU and applies
- *      batches with no host round trip inside a batch,
+ *      batches with no host round trip inside a batch;
+ *   2b. the batch engine: many resident graphs, one persistent launch per
+ *      step over all of them, snapshot/restore, and the autotuner;
+ *   2c. continuous batching: sliced steps and the request server;
  *   3. the reference's five step launchers on caller-owned device arrays in the
  *      reference's layout (drop-in for src/sparsifySubgraph.cu,
  *      src/connectedComponents.cu, src/labelInitialization.cu,
- *      src/iterativePropagation.cu of SMShovan/LabelPropCUDA).
+ *      src/iterativePropagation.cu of SMShovan/LabelPropCUDA), IrLP, and an
+ *      allocation-free propagation entry point;
+ *   4. device helpers (malloc/free/copies) for callers without a CUDA runtime.
  * The C++ shims in dynLP.h, sparsifySubgraph.h, connectedComponents.h,
  * labelInitialization.h and iterativePropagation.h call these.
  */
@@ -104,7 +109,8 @@ typedef struct dlp_config {
   int semantics;         /* enum dlp_semantics */
   int device;            /* CUDA device ordinal */
   int record;            /* nonzero: keep per-batch artefacts for dlp_session_artefact */
-  int narrow_lanes;      /* lanes per short row in propagation: 4, 8, 16 or 32; 0 = tuned */
+  int narrow_lanes;      /* lanes per short row in propagation: 4, 8, 16 or 32; 0 = 8
+                            (dlp_autotune picks one for a workload) */
   int blocks_per_sm;     /* persistent grid occupancy; 0 = from the occupancy query */
   double wait_timeout_s; /* limit for any device-side wait; <= 0: 2 s */
   int small_frontier_solo; /* bit 0: passes over small frontiers run on one

@@ -1,6 +1,8 @@
-// Device side of the resident session: the whole per-batch update of one
-// dynamic graph as ONE cooperative persistent kernel. Phases are separated by
-// grid barriers; nothing returns to the host inside a batch.
+// Per-graph device state and per-batch arguments of the batch engine
+// (engine.cuh, engine_kernel.cu). The whole per-batch update of a dynamic
+// graph runs inside ONE cooperative persistent launch, shared with the other
+// graphs of the step; phases are separated by grid barriers and nothing
+// returns to the host inside a batch.
 //
 // Reference path replaced (SMShovan/LabelPropCUDA, src/dynLP.cu:284-558):
 //   host rebuild + re-upload of the active CSR  -> phases A-C (incremental,
