@@ -430,7 +430,8 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     lanes, bps, tune = args.served_lanes, 0, None
     if lanes == 0:  # autotune the launch shape on a sample of the same size distribution
         sample = specs[:: max(1, len(specs) // 8)][:8]
-        tune = dlp.autotune([s[0] for s in sample], [s[1] for s in sample], batches=10, max_iterations=300)
+        tune = dlp.autotune([s[0] for s in sample], [s[1] for s in sample], batches=10, max_iterations=300,
+                            device=local_rank)
         lanes, bps = tune["narrow_lanes"], tune["blocks_per_sm"]
     eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=lanes, blocks_per_sm=bps)
     gids = [eng.add_problem(p) for p in probs]
