@@ -572,7 +572,7 @@ def main(argv=None) -> int:
                     "(default 20)")
     ap.add_argument("--served-lanes", type=int, default=0, help="0: autotune")
     ap.add_argument("--no-served", action="store_true")
-    ap.add_argument("--slice-us", type=float, default=1000.0)
+    ap.add_argument("--slice-us", type=float, default=2000.0)
     ap.add_argument("--plain-budget-s", type=float, default=20.0)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "gb300":

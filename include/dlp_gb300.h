@@ -306,7 +306,7 @@ int dlp_engine_in_progress(const dlp_engine *e, int graph_id);
 typedef struct dlp_server dlp_server;
 
 typedef struct {
-  double slice_us;            /* propagation time per step before waiting requests join (default 1000) */
+  double slice_us;            /* propagation time per step before waiting requests join (default 2000) */
   int pass_budget;            /* propagation passes per step (default 0: no limit) */
   size_t memory_budget_bytes; /* admission limit: the engine's resident bytes plus the device bytes of
                                  running requests (default 0: no limit) */

@@ -384,7 +384,7 @@ class Server:
     arrival order; each poll admits what fits and runs one sliced step over the
     admitted batches and those in progress. serial=True is the plain path."""
 
-    def __init__(self, engine: Engine, *, slice_us: float = 1000.0, pass_budget: int = 0,
+    def __init__(self, engine: Engine, *, slice_us: float = 2000.0, pass_budget: int = 0,
                  memory_budget_bytes: int = 0, max_batches_per_step: int = 0, serial: bool = False):
         L = _n.lib()
         cfg = _n.ServerConfig()

@@ -38,6 +38,13 @@ __global__ void interleave_kernel(const int *col, const float *val, int2 *adj, i
     adj[i] = make_int2(col[i], __float_as_int(val[i]));
 }
 
+// Every row empty: {row start, 0}.
+__global__ void rowinfo_reset_kernel(const int *full_row, int2 *rowinfo, int64_t n) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    rowinfo[i] = make_int2(full_row[i], 0);
+}
+
 __global__ void fill_f32_kernel(float *p, float v, int64_t count) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
@@ -74,7 +81,7 @@ int dalloc(T **p, size_t count, std::vector<void *> &owned, size_t &counted, std
 // Device bytes a resident graph needs (fixed part).
 size_t graph_bytes(int64_t n, int64_t m, bool truth, bool bmap, bool record) {
   size_t b = 4 * (n + 1) + 16 * m + 4 * n + 2 * n + 4 * n + 8 * n + 4 * n + 16 * n + 4 * n * 2 + 4 * n * 5 +
-             4 * n + 16 * n + n + sizeof(dlp_batch_stats) * kStepRing;
+             4 * n + 16 * n + n + 8 * n + sizeof(dlp_batch_stats) * kStepRing;
   if (truth) b += n;
   if (bmap) b += 4 * n;
   if (record) b += 4 * n * 4 + 4 * dlp::session::kRecordIters;
@@ -243,6 +250,7 @@ int reset_graph(dlp_engine *e, GraphSlot *g, int gid) {
   DLP_CUDA_TRY(cudaMemsetAsync(d.local, 0xff, sizeof(int) * n, q));
   for (unsigned *p : {d.del_stamp, d.gt_stamp, d.dirty_stamp, d.front_stamp})
     DLP_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(unsigned) * n, q));
+  rowinfo_reset_kernel<<<1024, 256, 0, q>>>(d.full_row, d.rowinfo, n);
   fill_f32_kernel<<<1024, 256, 0, q>>>(d.lab0, 0.5f, n);
   fill_f32_kernel<<<1024, 256, 0, q>>>(d.lab1, 0.5f, n);
   DLP_CUDA_TRY(cudaGetLastError());
@@ -516,7 +524,7 @@ int alloc_graph(dlp_engine *e, int n, int64_t m, bool with_truth, bool with_bmap
       (st = dalloc(&d.flist, 3 * static_cast<size_t>(n), o, b, z)) ||
       (st = dalloc(&d.touched, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&d.par, n, o, b, z)) ||
       (st = dalloc(&d.acc, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&g->stats, kStepRing, o, b, z)) ||
-      (st = dalloc(&d.nmeta, n, o, b, z)) ||
+      (st = dalloc(&d.nmeta, n, o, b, z)) || (st = dalloc(&d.rowinfo, n, o, b, z)) ||
       (with_truth && (st = dalloc(&truth, n, o, b, z))) || (with_bmap && (st = dalloc(&bmap, n, o, b, z))) ||
       (e->cfg.record &&
        ((st = dalloc(&d.rec_front0, n, o, b, z)) || (st = dalloc(&d.rec_root, n, o, b, z)) ||

@@ -400,6 +400,7 @@ __device__ void phase_c(const EngineArgs &e, const Ctx &c, int *pref) {
     if (valid && gl == 0) {
       const int len = keep_row ? pos : 0;
       s.act_len[u] = len;
+      s.rowinfo[u] = make_int2(rs, len);
       s.nmeta[u] = static_cast<uint8_t>((s.gt[u] < 0 ? 1 : 0) | (len > kNarrowMax ? 2 : 0));
     }
   });
@@ -719,8 +720,9 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
   int rs = 0, len = 0;
   float old = 0.0f;
   if (valid) {
-    rs = s.full_row[u];
-    len = s.act_len[u];
+    const int2 ri = s.rowinfo[u];
+    rs = ri.x;
+    len = ri.y;
     if (gl == 0) old = src[u];
   }
   float sw[R], sl[R];
@@ -833,8 +835,9 @@ __device__ __forceinline__ void group_mark(const GV &w, const int (&cand)[32 / G
 template <class Mark>
 __device__ __forceinline__ void wide_row(const DevState &s, const float *src, float *dst, float delta, int u,
                                          int lane, Mark mark) {
-  const int rs = s.full_row[u];
-  const int len = s.act_len[u];
+  const int2 ri = s.rowinfo[u];
+  const int rs = ri.x;
+  const int len = ri.y;
   float sw[8], sl[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) sw[j] = sl[j] = 0.0f;

@@ -322,7 +322,7 @@ extern "C" {
 void dlp_server_config_default(dlp_server_config *cfg) {
   if (!cfg) return;
   std::memset(cfg, 0, sizeof(*cfg));
-  cfg->slice_us = 1000.0;
+  cfg->slice_us = 2000.0;
 }
 
 int dlp_server_create(dlp_engine *e, const dlp_server_config *cfg, dlp_server **out) {

@@ -63,6 +63,7 @@ struct DevState {
   const int2 *full_adj;     // {col, weight bits}, full graph
   int2 *act_adj;            // live rows, same slots as full_adj
   int *act_len;             // live row length
+  int2 *rowinfo;            // {row start, live row length}: what a propagation pass reads, in one load
   int8_t *status;           // host-side status (src/dynLP.cu:117-130)
   int8_t *gt;               // -1 / 0 / 1
   uint8_t *nmeta;           // what propagation needs about a neighbour, in one byte:
