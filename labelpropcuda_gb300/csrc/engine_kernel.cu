@@ -1534,7 +1534,7 @@ __device__ void phase_h(const EngineArgs &e, const Ctx &c, int *pref, int k_end)
 }  // namespace
 
 template <int G>
-__global__ void __launch_bounds__(kBlock, 2) engine_kernel(EngineArgs e) {
+__global__ void __launch_bounds__(kBlock, 1024 / kBlock) engine_kernel(EngineArgs e) {
   const Ctx c = make_ctx();
   __shared__ int pref[kMaxGraphs + 1];
   __shared__ int pref2[kMaxGraphs + 1];

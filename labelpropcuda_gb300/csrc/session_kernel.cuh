@@ -22,7 +22,11 @@
 namespace dlp {
 namespace session {
 
-constexpr int kBlock = 512;
+#ifndef DLP_BLOCK
+#define DLP_BLOCK 1024
+#endif
+constexpr int kBlock = DLP_BLOCK;       // threads per block of the persistent kernel (512 or 1024)
+static_assert(kBlock == 512 || kBlock == 1024, "the persistent kernel is tuned for 512 or 1024 threads");
 constexpr int kMaxHookRounds = 100;     // the reference's outer SV cap (src/connectedComponents.cu:209)
 constexpr int kRecordIters = 1 << 17;   // per-pass frontier sizes kept when recording
 constexpr int kNarrowMax = 32;          // rows up to this length use the group path
