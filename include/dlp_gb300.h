@@ -257,7 +257,7 @@ int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, 
  * Propagation sends rows of at most 32 live entries to groups of
  * narrow_lanes lanes and longer rows to whole warps; the lane width of that
  * short-row bucket and the persistent grid's blocks per SM are chosen by
- * timing every candidate (lanes 4/8/16 x 2 or 1 blocks per SM) on a sample the
+ * timing every candidate (lanes 4/8/16 x the blocks per SM the build allows) on a sample the
  * library generates with the reference generator: num_graphs graphs of
  * sizes[i] vertices and average degree degrees[i], `batches` batches each,
  * propagation capped at max_iterations passes per batch for the trial. Every

@@ -16,7 +16,7 @@
 #include <memory>
 #include <vector>
 
-#include "common.cuh"
+#include "session_kernel.cuh"
 
 namespace {
 
@@ -109,7 +109,9 @@ int dlp_autotune(dlp_config *cfg, int num_graphs, const int *sizes, const int *d
     bmaps.push_back(std::move(m));
   }
   static const int kLanes[] = {4, 8, 16};
-  static const int kBlocks[] = {2, 1};
+  // blocks per SM the build's block size allows (1024-thread blocks: one)
+  std::vector<int> kBlocks = {1};
+  if (dlp::session::kBlock <= 512) kBlocks.insert(kBlocks.begin(), 2);
   dlp_tune_report rep;
   std::memset(&rep, 0, sizeof(rep));
   std::vector<dlp_batch_stats> ref_stats;

@@ -89,7 +89,8 @@ def test_autotune_picks_a_measured_candidate(gpu):
     must agree on the statistics (checked inside) and the choice is the
     fastest measured one."""
     r = dlp.autotune([3000, 1000, 2000], [5, 3, 7], batches=5, max_iterations=300)
-    assert len(r["candidates"]) == 6
+    shapes = {(c["narrow_lanes"], c["blocks_per_sm"]) for c in r["candidates"]}
+    assert len(shapes) == len(r["candidates"]) >= 3  # every candidate a distinct launch shape
     assert all(c["ms"] > 0 for c in r["candidates"])
     best = min(r["candidates"], key=lambda c: c["ms"])
     assert (r["narrow_lanes"], r["blocks_per_sm"]) == (best["narrow_lanes"], best["blocks_per_sm"])
