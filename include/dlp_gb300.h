@@ -226,6 +226,11 @@ int dlp_engine_snapshot(dlp_engine *e, int graph_id, void *out, size_t capacity,
  * the same record flag and semantics; counts against the memory budget like
  * dlp_engine_add_graph. *graph_id receives its (possibly new) id. */
 int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *graph_id);
+/* Same, into the given free graph id (so a graph can keep its id across an
+ * eviction). */
+int dlp_engine_restore_as(dlp_engine *e, const void *snapshot, size_t bytes, int graph_id);
+/* Device bytes a resident graph occupies (0 for an unknown id). */
+size_t dlp_engine_graph_resident_bytes(const dlp_engine *e, int graph_id);
 int dlp_engine_reset_graph(dlp_engine *e, int graph_id);
 float dlp_engine_tau(const dlp_engine *e, int graph_id);
 void *dlp_engine_stream(dlp_engine *e);
@@ -312,6 +317,9 @@ typedef struct {
                                  running requests (default 0: no limit) */
   int max_batches_per_step;   /* new batches started per step (default 0: the engine's max_graphs) */
   int serial;                 /* 1: the plain path, one request at a time run to its end (default 0) */
+  int evict_idle;             /* 1: when a request does not fit the budget, graphs with no request
+                                 running are evicted to host memory (least recently used first) and
+                                 restored under the same id before their next request (default 0) */
 } dlp_server_config;
 void dlp_server_config_default(dlp_server_config *cfg);
 
@@ -352,6 +360,11 @@ int dlp_server_poll(dlp_server *s, int *completed_ids, int capacity, int *num_co
 int dlp_server_result(const dlp_server *s, int request_id, dlp_request_result *out);
 /* Requests queued or running. */
 int dlp_server_pending(const dlp_server *s);
+/* Graphs this server evicted to host memory and restored so far. */
+int dlp_server_evictions(const dlp_server *s, int *evictions, int *restores);
+/* Restores graph_id if this server evicted it (evicting others if allowed and
+ * needed), so that the engine's calls can reach it again. */
+int dlp_server_make_resident(dlp_server *s, int graph_id);
 /* Replays a trace in real time: reqs[i] (sorted by arrival_s) is submitted
  * once arrival_s seconds have passed since the call began, and the server
  * polls until every request has ended. out[i] holds request i's result with

@@ -385,13 +385,15 @@ class Server:
     admitted batches and those in progress. serial=True is the plain path."""
 
     def __init__(self, engine: Engine, *, slice_us: float = 2000.0, pass_budget: int = 0,
-                 memory_budget_bytes: int = 0, max_batches_per_step: int = 0, serial: bool = False):
+                 memory_budget_bytes: int = 0, max_batches_per_step: int = 0, serial: bool = False,
+                 evict_idle: bool = False):
         L = _n.lib()
         cfg = _n.ServerConfig()
         L.dlp_server_config_default(ctypes.byref(cfg))
         cfg.slice_us, cfg.pass_budget = slice_us, pass_budget
         cfg.memory_budget_bytes, cfg.max_batches_per_step, cfg.serial = memory_budget_bytes, max_batches_per_step, \
             int(bool(serial))
+        cfg.evict_idle = int(bool(evict_idle))
         self.engine = engine
         self._h = ctypes.c_void_p()
         _n.check(L.dlp_server_create(engine._h, ctypes.byref(cfg), ctypes.byref(self._h)))
@@ -417,6 +419,15 @@ class Server:
     @property
     def pending(self) -> int:
         return int(_n.lib().dlp_server_pending(self._h))
+
+    def evictions(self) -> tuple[int, int]:
+        """(graphs evicted to host memory, graphs restored) so far."""
+        ev, rs = ctypes.c_int(0), ctypes.c_int(0)
+        _n.check(_n.lib().dlp_server_evictions(self._h, ctypes.byref(ev), ctypes.byref(rs)))
+        return ev.value, rs.value
+
+    def make_resident(self, gid: int) -> None:
+        _n.check(_n.lib().dlp_server_make_resident(self._h, gid))
 
     def drain(self) -> list[int]:
         done = []

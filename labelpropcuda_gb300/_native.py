@@ -56,7 +56,7 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [
         ("slice_us", ctypes.c_double), ("pass_budget", ctypes.c_int),
         ("memory_budget_bytes", ctypes.c_size_t), ("max_batches_per_step", ctypes.c_int),
-        ("serial", ctypes.c_int),
+        ("serial", ctypes.c_int), ("evict_idle", ctypes.c_int),
     ]
 
 
@@ -161,6 +161,10 @@ _SIGNATURES = {
     "dlp_engine_graph_nodes": (_I, [_P, _I]),
     "dlp_engine_snapshot": (_I, [_P, _I, _P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "dlp_engine_restore": (_I, [_P, _P, ctypes.c_size_t, c_int_p]),
+    "dlp_engine_restore_as": (_I, [_P, _P, ctypes.c_size_t, _I]),
+    "dlp_engine_graph_resident_bytes": (ctypes.c_size_t, [_P, _I]),
+    "dlp_server_evictions": (_I, [_P, c_int_p, c_int_p]),
+    "dlp_server_make_resident": (_I, [_P, _I]),
     "dlp_autotune": (_I, [ctypes.POINTER(Config), _I, c_int_p, c_int_p, _I, _I, ctypes.POINTER(TuneReport)]),
     "dlp_engine_reserve": (_I, [_P, _I, _I, _I]),
     "dlp_server_reserve": (_I, [_P, _I, _I, _I, _I, _I]),

@@ -804,9 +804,10 @@ int dlp_engine_snapshot(dlp_engine *e, int graph_id, void *out, size_t capacity,
   return DLP_OK;
 }
 
-int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *graph_id) {
-  dlp::clear_error();
-  if (!e || !snapshot || !graph_id) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+namespace {
+// Restores into graph id `want` (a free id), or into the first free id when
+// want < 0.
+int restore_graph(dlp_engine *e, const void *snapshot, size_t bytes, int want, int *graph_id) {
   *graph_id = -1;
   SnapHeader h{};
   if (bytes < sizeof(h)) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "snapshot too short");
@@ -820,11 +821,17 @@ int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *g
   if (e->budget > 0 && e->used + need > e->budget)
     return dlp::fail(DLP_ERR_OUT_OF_MEMORY, "graph does not fit the engine's device-memory budget");
   int gid = -1;
-  for (int i = 0; i < e->max_graphs; ++i)
-    if (!e->graphs[i]) {
-      gid = i;
-      break;
-    }
+  if (want >= 0) {
+    if (want >= e->max_graphs || e->graphs[want])
+      return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "graph id " + std::to_string(want) + " is not free");
+    gid = want;
+  } else {
+    for (int i = 0; i < e->max_graphs; ++i)
+      if (!e->graphs[i]) {
+        gid = i;
+        break;
+      }
+  }
   if (gid < 0) return dlp::fail(DLP_ERR_OUT_OF_MEMORY, "the engine holds max_graphs graphs already");
   DLP_CUDA_TRY(cudaSetDevice(e->device));
   GraphSlot *g = nullptr;
@@ -870,6 +877,25 @@ int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *g
   e->used += g->bytes;
   *graph_id = gid;
   return DLP_OK;
+}
+}  // namespace
+
+int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *graph_id) {
+  dlp::clear_error();
+  if (!e || !snapshot || !graph_id) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+  return restore_graph(e, snapshot, bytes, -1, graph_id);
+}
+
+int dlp_engine_restore_as(dlp_engine *e, const void *snapshot, size_t bytes, int graph_id) {
+  dlp::clear_error();
+  if (!e || !snapshot || graph_id < 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument or negative id");
+  int got = -1;
+  return restore_graph(e, snapshot, bytes, graph_id, &got);
+}
+
+size_t dlp_engine_graph_resident_bytes(const dlp_engine *e, int graph_id) {
+  GraphSlot *g = slot_of(const_cast<dlp_engine *>(e), graph_id);
+  return g ? g->bytes : 0;
 }
 
 int dlp_engine_reset_graph(dlp_engine *e, int graph_id) {

@@ -70,13 +70,19 @@ struct Request {
   dlp_request_result res{};
 };
 
-// Per-graph device copy of its running batch (grown, reused).
+// Per-graph device copy of its running batch (grown, reused), and the graph's
+// eviction state.
 struct GraphBuf {
   char *dev = nullptr;
   size_t dev_cap = 0;
   char *pinned = nullptr;
   size_t pin_cap = 0;
   int running = -1;  // request id
+  bool evicted = false;
+  std::vector<char> snap;  // the graph's device state while evicted
+  size_t graph_bytes = 0;  // its device bytes when resident
+  int nodes = 0;
+  double last_use = 0.0;
 };
 
 size_t batch_bytes(const dlp_batch_view &v) {
@@ -84,8 +90,7 @@ size_t batch_bytes(const dlp_batch_view &v) {
          align16(4 * static_cast<size_t>(v.num_deleted)) + 3 * align16(4 * static_cast<size_t>(v.num_edges));
 }
 
-int check_request(dlp_engine *e, const dlp_request &r) {
-  const int n = dlp_engine_graph_nodes(e, r.graph_id);
+int check_request(int n, const dlp_request &r) {
   if (n <= 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "request for an unknown graph id");
   const dlp_batch_view &v = r.batch;
   if (v.num_inserted < 0 || v.num_gt < 0 || v.num_deleted < 0 || v.num_edges < 0)
@@ -115,6 +120,7 @@ struct dlp_server {
   std::vector<GraphBuf> bufs;
   size_t running_bytes = 0;
   int running = 0;
+  int evictions = 0, restores = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
@@ -130,8 +136,71 @@ struct dlp_server {
     }
   }
 
+  // Vertex count of a graph resident in the engine or evicted by this server.
+  int graph_nodes(int gid) {
+    const int n = dlp_engine_graph_nodes(eng, gid);
+    if (n > 0) return n;
+    if (gid >= 0 && gid < static_cast<int>(bufs.size()) && bufs[gid].evicted) return bufs[gid].nodes;
+    return -1;
+  }
+
+  // Evicts graph gid: its whole device state to host memory, then its device
+  // memory freed. Only for a graph with no batch in progress.
+  int evict(int gid) {
+    GraphBuf &b = buf(gid);
+    size_t bytes = 0;
+    DLP_TRY(dlp_engine_snapshot(eng, gid, nullptr, 0, &bytes));
+    b.snap.resize(bytes);
+    DLP_TRY(dlp_engine_snapshot(eng, gid, b.snap.data(), bytes, &bytes));
+    b.graph_bytes = dlp_engine_graph_resident_bytes(eng, gid);
+    b.nodes = dlp_engine_graph_nodes(eng, gid);
+    DLP_TRY(dlp_engine_remove_graph(eng, gid));
+    b.evicted = true;
+    ++evictions;
+    return DLP_OK;
+  }
+
+  int restore(int gid) {
+    GraphBuf &b = buf(gid);
+    DLP_TRY(dlp_engine_restore_as(eng, b.snap.data(), b.snap.size(), gid));
+    b.snap.clear();
+    b.snap.shrink_to_fit();
+    b.evicted = false;
+    ++restores;
+    return DLP_OK;
+  }
+
+  // Bytes the budget counts: resident graphs plus running requests.
+  bool fits(size_t need) const {
+    return cfg.memory_budget_bytes == 0 ||
+           dlp_engine_bytes_in_use(eng) + running_bytes + need <= cfg.memory_budget_bytes;
+  }
+
+  // Evicts idle resident graphs, least recently used first (never `keep` nor
+  // a graph in `busy`), until `need` more bytes fit. Returns whether they do.
+  int make_room(size_t need, int keep, const std::vector<int> &busy, bool *ok) {
+    *ok = fits(need);
+    while (!*ok && cfg.evict_idle) {
+      int victim = -1;
+      for (int g = 0; g < dlp::engine::kMaxGraphs; ++g) {
+        if (g == keep || dlp_engine_graph_nodes(eng, g) <= 0) continue;
+        if (g < static_cast<int>(bufs.size()) && bufs[g].running >= 0) continue;
+        if (std::find(busy.begin(), busy.end(), g) != busy.end()) continue;
+        const double lu = g < static_cast<int>(bufs.size()) ? bufs[g].last_use : 0.0;
+        if (victim < 0 || lu < bufs[victim].last_use) {
+          buf(g);  // the victim needs an entry for its snapshot
+          victim = g;
+        }
+      }
+      if (victim < 0) break;
+      DLP_TRY(evict(victim));
+      *ok = fits(need);
+    }
+    return DLP_OK;
+  }
+
   int enqueue(const dlp_request &r, bool copy, double arrival, int *id) {
-    DLP_TRY(check_request(eng, r));
+    DLP_TRY(check_request(graph_nodes(r.graph_id), r));
     Request q;
     q.gid = r.graph_id;
     q.batch = r.batch_index;
@@ -221,7 +290,6 @@ struct dlp_server {
     std::vector<int> gids, bidx, admitted;
     std::vector<dlp_batch_view> dv;
     std::vector<char> blocked;
-    const size_t resident = dlp_engine_bytes_in_use(eng);
     int out_n = 0;
     auto report = [&](int id) {
       if (completed && out_n < capacity) completed[out_n] = id;
@@ -238,8 +306,12 @@ struct dlp_server {
         ++it;
         continue;
       }
-      if (cfg.memory_budget_bytes > 0 && resident + running_bytes + r.bytes > cfg.memory_budget_bytes) {
-        if (resident + r.bytes > cfg.memory_budget_bytes) {  // can never fit
+      // an evicted graph needs its own bytes back as well
+      const size_t need = r.bytes + (b.evicted ? b.graph_bytes : 0);
+      bool ok = true;
+      DLP_TRY(make_room(need, r.gid, gids, &ok));
+      if (!ok) {
+        if (running == 0 && gids.empty()) {  // nothing will free bytes: it can never fit
           dlp::set_error("request does not fit the memory budget");
           finish(r, DLP_ERR_OUT_OF_MEMORY, now());
           report(*it);
@@ -250,6 +322,8 @@ struct dlp_server {
         ++it;
         continue;
       }
+      if (b.evicted) DLP_TRY(restore(r.gid));
+      b.last_use = t_admit;
       dlp_batch_view v;
       DLP_TRY(stage(r, b, &v));
       b.running = *it;
@@ -389,6 +463,25 @@ int dlp_server_result(const dlp_server *s, int request_id, dlp_request_result *o
   return DLP_OK;
 }
 
+int dlp_server_evictions(const dlp_server *s, int *evictions, int *restores) {
+  dlp::clear_error();
+  if (!s) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null server");
+  if (evictions) *evictions = s->evictions;
+  if (restores) *restores = s->restores;
+  return DLP_OK;
+}
+
+int dlp_server_make_resident(dlp_server *s, int graph_id) {
+  dlp::clear_error();
+  if (!s || s->graph_nodes(graph_id) <= 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph id");
+  GraphBuf &b = s->buf(graph_id);
+  if (!b.evicted) return DLP_OK;
+  bool ok = true;
+  DLP_TRY(s->make_room(b.graph_bytes, graph_id, {}, &ok));
+  if (!ok) return dlp::fail(DLP_ERR_OUT_OF_MEMORY, "the graph does not fit the memory budget");
+  return s->restore(graph_id);
+}
+
 int dlp_server_pending(const dlp_server *s) { return s ? static_cast<int>(s->queue.size()) + s->running : 0; }
 
 int dlp_server_replay(dlp_server *s, int count, const dlp_request *reqs, dlp_request_result *out,
@@ -398,7 +491,7 @@ int dlp_server_replay(dlp_server *s, int count, const dlp_request *reqs, dlp_req
   for (int i = 1; i < count; ++i)
     if (reqs[i].arrival_s < reqs[i - 1].arrival_s)
       return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "requests must be sorted by arrival time");
-  for (int i = 0; i < count; ++i) DLP_TRY(check_request(s->eng, reqs[i]));
+  for (int i = 0; i < count; ++i) DLP_TRY(check_request(s->graph_nodes(reqs[i].graph_id), reqs[i]));
   std::vector<int> ids(count, -1);
   const double base = s->now();
   int next = 0, done = 0;

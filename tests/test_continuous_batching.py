@@ -222,3 +222,34 @@ def test_snapshot_evict_restore_continues_identically(gpu):
     a.step([(filler, 0, dlp.Problem(1000, 3, 5, 7).batches[0])])
     with pytest.raises(dlp.DlpError):
         dlp.Engine(1, max_iterations=MAX_ITER, semantics=dlp.SEMANTICS_SPEC).restore(snap)
+
+
+@pytest.mark.gpu
+def test_server_evicts_idle_graphs_to_fit_the_budget(gpu):
+    """Five resident graphs under a budget that holds about two of them: the
+    server evicts idle graphs to host memory and restores them (same ids)
+    when their requests come; every result equals the graph run alone."""
+    probs = [dlp.Problem(*g) for g in GRAPHS]
+    want = [alone(p) for p in probs]
+    eng = dlp.Engine(len(probs), max_iterations=MAX_ITER)
+    gids = [eng.add_problem(p) for p in probs]
+    L = N.lib()
+    sizes = sorted(int(L.dlp_engine_graph_resident_bytes(eng._h, g)) for g in gids)
+    biggest_req = max(24 * bt.edge_src.size + bt.nbytes() + 8 * bt.deleted.size + 4096
+                      for p in probs for bt in p.batches)
+    budget = sizes[-1] + sizes[-2] + 4 * biggest_req
+    assert sum(sizes) > budget  # not everything fits at once
+    srv = dlp.Server(eng, slice_us=50.0, memory_budget_bytes=budget, evict_idle=True)
+    trace = _trace(probs, gids, 5, 0.05)
+    res, _ = srv.replay(trace)
+    for (t, gid, b, _), r in zip(trace, res):
+        i = gids.index(gid)
+        assert r["status"] == 0, r
+        same(r["stats"], want[i][b][0], ("evict", i, b))
+    ev, rs = srv.evictions()
+    assert ev > 0 and rs > 0
+    assert eng.bytes_in_use <= budget
+    for i, gid in enumerate(gids):
+        srv.make_resident(gid)
+        assert eng.labels(gid).tobytes() == want[i][-1][1].tobytes()
+    srv.close()
