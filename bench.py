@@ -189,6 +189,39 @@ def percentile(xs, q):
 
 # -------------------------------------------------------------- CPU (oracle) --
 
+def host_cpu() -> dict:
+    """CPU model and core count of this host (the CPU baselines' hardware)."""
+    model = None
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            k, _, v = ln.partition(":")
+            if k.strip() in ("model name", "Model"):
+                model = v.strip()
+                break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for ln in out.splitlines():
+                if ln.startswith("Model name:"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    return {"model": model or "unknown", "nproc": os.cpu_count() or 1}
+
+
+def oracle_problem(w: dict, batches: int = 0):
+    """The workload's inputs from the oracle's own generator (no product code)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    p = pyoracle.OracleProblem(w["n"], w["degree"], w["batches"], w["seed"])
+    if batches > 0:
+        p.batches = p.batches[:batches]
+    return p
+
+
 def cpu_run(problem, threads: int, budget_s: float):
     """Oracle replay in batch order until the budget is used; returns
     (affected edges, seconds, batches done)."""
@@ -204,15 +237,67 @@ def cpu_run(problem, threads: int, budget_s: float):
     return edges, time.perf_counter() - t0, done
 
 
+def fp64_error(problem, gpu_labels, threads: int) -> dict:
+    """The FP32 path against the FP64 oracle on the same workload: the
+    oracle's fp32 run (which the GPU's final labels must equal bit for bit)
+    with each batch's propagation repeated in double from the same state."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    run = pyoracle.OracleRun.from_problem(problem, threads=threads, fp64=2)
+    per = []
+    for b, bt in enumerate(problem.batches):
+        st = run.apply(b, bt)
+        l32, l64 = run.labels().astype(np.float64), run.labels64()
+        err = np.abs(l32 - l64)
+        per.append({"batch": b, "max_abs": float(err.max()), "p999_abs": float(np.percentile(err, 99.9)),
+                    "prediction_flips": int(np.sum((l32 >= 0.5) != (l64 >= 0.5))),
+                    "fp32_passes": st["iterations"], "fp64_passes": run.shadow_iterations()})
+    return {"max_abs": max(r["max_abs"] for r in per), "prediction_flips_max": max(r["prediction_flips"] for r in per),
+            "gpu_labels_equal_oracle_fp32": bool(np.array_equal(gpu_labels, run.labels())),
+            "per_batch": per,
+            "how": "oracle fp32 schedule vs the same batch's propagation in double from the same state"}
+
+
+def reference_cuda(w: dict, batches: int, our_stats: list) -> dict | None:
+    """The reference's own CUDA build (its runDynLP, launchers and kernels,
+    -O3 --use_fast_math, from the guarded source copy) timed on this GPU on
+    the same workload; None when oracle/_ref/ref_kernels is absent."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import tempfile
+    import pyoracle
+    if not pyoracle.REF_KERNELS.exists():
+        return None
+    nb = batches or w["batches"]
+    with tempfile.TemporaryDirectory() as td:
+        t0 = time.perf_counter()
+        r = pyoracle.run_ref_kernels(w["n"], w["degree"], nb, w["seed"], 100000, Path(td) / "ref.bin",
+                                     record=False)
+        wall = time.perf_counter() - t0
+    ms = [float(x) for x in r["batch_ms"]]
+    its = [b["iterations"] for b in r["batches"]]
+    same = its == [s["iterations"] for s in our_stats]
+    out = {"batch_ms": ms, "ms_per_replay": sum(ms), "batch_ms_p50": percentile(ms, 0.5),
+           "batch_ms_p99": percentile(ms, 0.99), "iterations": its, "iterations_match": same,
+           "process_wall_s": wall,
+           "timing": "the reference's own per-batch CUDA events (src/dynLP.cu:285,547-552: host CSR rebuild, "
+                     "uploads, kernels, label read-back and host accuracy), sm_103a build of its sources"}
+    if same:
+        out["value"] = sum(s["affected_edges"] for s in our_stats) / (sum(ms) / 1e3)
+        out["unit"] = UNIT + " (affected edges counted by the oracle: identical pass counts)"
+    return out
+
+
 def reference_arm(args, td, rank):
-    import labelpropcuda_gb300 as dlp
+    """The reference has no CPU implementation of its path (it is CUDA only),
+    so this arm times the oracle's restatement of it on every host thread, on
+    inputs from the oracle's own generator: nothing of the product is loaded."""
     if rank != 0:
         return 0
     w = WORKLOADS[args.workload]
-    p = dlp.Problem(w["n"], w["degree"], w["batches"], w["seed"])
-    if args.batches > 0:
-        p.batches = p.batches[:args.batches]
-    threads = os.cpu_count() or 1
+    p = oracle_problem(w, args.batches)
+    cpu = host_cpu()
+    threads = cpu["nproc"]
     for _ in range(args.warmup):
         cpu_run(p, threads, args.ref_budget_s)
     tot_e, tot_t, per = 0, 0.0, []
@@ -224,14 +309,16 @@ def reference_arm(args, td, rank):
         per.append(t)
         batches_done = done
     value = tot_e / tot_t if tot_t > 0 else 0.0
-    sample = (f"oracle port (CPU restatement of the reference's per-batch path), {threads} threads, "
-              f"first {batches_done} of {w['batches']} batches per step (budget {args.ref_budget_s:.0f} s)")
+    sample = (f"oracle port (CPU restatement of the reference's per-batch path), {threads} threads on "
+              f"{cpu['model']} ({cpu['nproc']} cores), first {batches_done} of {w['batches']} batches per step "
+              f"(budget {args.ref_budget_s:.0f} s)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic (reference generator decisions, seed 42)",
             "config": {"workload": workload_desc(args.workload, args.batches), "semantics": "ref"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "cpu_model": cpu["model"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -334,6 +421,17 @@ def gpu_arm(args, td, rank, world, local_rank):
             traffic = None
     # CPU baseline: the oracle, single thread, bounded sample of the same workload
     cpu_edges, cpu_t, cpu_done = cpu_run(p, 1, args.cpu_budget_s)
+    cpu = host_cpu()
+    # FP64 oracle error on this workload, and the reference's own CUDA build
+    progress("fp64 oracle")
+    fp64 = fp64_error(p, sess.labels(), cpu["nproc"])
+    ref_cuda = None
+    if not args.no_reference_cuda:
+        progress("reference CUDA build")
+        try:
+            ref_cuda = reference_cuda(w, args.batches, stats0)
+        except Exception as exc:  # reported, not fatal: it is a baseline
+            ref_cuda = {"error": repr(exc)[:300]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
@@ -350,10 +448,13 @@ def gpu_arm(args, td, rank, world, local_rank):
                 "timing": "wall clock, stream synchronised on both sides"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "kernel": "dlp::engine::engine_kernel<8>", "peak_source": peak_kind,
+                     "kernel": f"dlp::engine_kernel<{args.lanes or 8}>", "peak_source": peak_kind,
                      "algorithmic_bytes_per_step": bytes_step},
         "cpu_baseline": {"value": cpu_edges / cpu_t if cpu_t > 0 else 0.0, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"oracle port, 1 thread, first {cpu_done} of {nb} batches of the same workload"},
+                         "sample": f"oracle port, 1 thread, first {cpu_done} of {nb} batches of the same workload",
+                         "cpu_model": cpu["model"], "host_cores": cpu["nproc"]},
+        "fp64_oracle_error": fp64,
+        "reference_cuda": ref_cuda,
         "clocks": clocks,
         "gpu_launches": args.steps * nb * 2,
     }
@@ -402,13 +503,49 @@ def progress(msg: str) -> None:
     print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
+def stratified_plain(sizes_n, plain_time, per_stratum: int, bins: int, seed: int):
+    """Stratified sample of whole graphs for the plain path: graphs binned by
+    log(vertex count) into `bins` equal-width strata, `per_stratum` graphs
+    drawn per stratum (seeded), each replayed serially by plain_time(index) ->
+    seconds. Returns (estimated total seconds for all graphs, its standard
+    error, graphs sampled): the stratified estimator sum_h N_h * mean_h with
+    the finite-population correction."""
+    import numpy as np
+    logs = np.log(np.asarray(sizes_n, dtype=np.float64))
+    edges = np.linspace(logs.min(), logs.max() + 1e-9, bins + 1)
+    strata = np.clip(np.digitize(logs, edges) - 1, 0, bins - 1)
+    rng = np.random.default_rng(seed)
+    total, var, sampled = 0.0, 0.0, []
+    for h in range(bins):
+        members = np.flatnonzero(strata == h)
+        if members.size == 0:
+            continue
+        k = min(per_stratum, members.size)
+        pick = rng.choice(members, size=k, replace=False)
+        t = np.array([plain_time(int(i)) for i in pick])
+        sampled += [int(i) for i in pick]
+        total += members.size * t.mean()
+        if k > 1:
+            var += members.size ** 2 * (1.0 - k / members.size) * t.var(ddof=1) / k
+    return total, float(np.sqrt(var)), sampled
+
+
 def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
-    """The mixed-graph stream: N resident graphs, every graph's 10 batches.
-    batched = one engine step per batch index over all graphs (one launch per
-    step, per-graph convergence); served = the continuous-batching server
-    replaying the requests (all queued at once = saturation, then Poisson at
-    half that request rate); plain = the same server in serial mode (one
-    request at a time, run to its end), on a bounded sample of the trace.
+    """Served vs plain over the mixed-graph stream. Default: the multi-instance
+    configuration, 512 graphs with n log-uniform on [1e3, 5e5] (numpy PCG64
+    seed 1000003), degree {3,5,7}[i mod 3], generator seed i, every graph's
+    10 batches as 5,120 requests in batch-major order.
+      batched          one engine launch per batch index over every graph
+      served_saturated the continuous-batching server with every request
+                       queued at t = 0 (host-to-device copies included)
+      served_poisson   the same server with Poisson arrivals at fractions of
+                       the saturated request rate, each over a fixed window of
+                       arrivals (a prefix of the request list, so every graph's
+                       batches keep their order); latency = finish - arrival
+      plain            the server in serial mode (one request at a time, run
+                       to its end: the plain per-batch path) replaying the same
+                       requests graph by graph, on a stratified sample of whole
+                       graphs (strata by log size), scaled to all graphs
     With several ranks each serves its shard of the graphs (shard_graphs);
     rates are summed over ranks and times take the slowest rank."""
     import numpy as np
@@ -419,21 +556,23 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
         # serving-stream shape: larger graphs, requests of about 2% of a graph
         # (40 batches per graph); every graph first takes its first `skip`
         # batches (untimed), then --served-batches more are served
-        lo, hi, count, gen_batches, nb = 1e4, 5e6, args.served_graphs, 40, args.served_batches
+        lo, hi, count, gen_batches, nb = 1e4, 5e6, args.served_graphs or 256, 40, args.served_batches
         skip = 20 if args.served_skip < 0 else args.served_skip
     else:
-        lo, hi, count, gen_batches, nb = 1e3, 5e5, args.served_graphs, 10, 10
+        lo, hi, count, gen_batches, nb = 1e3, 5e5, args.served_graphs or 512, 10, 10
         skip = 0
     all_specs = [(n, d, gen_batches, sd) for n, d, _, sd in mix_sizes(count, lo, hi, 1000003)]
-    specs = [all_specs[i] for i in shard_graphs(all_specs, rank, world)]
+    mine = shard_graphs(all_specs, rank, world)
+    specs = [all_specs[i] for i in mine]
     probs = make_problems(specs, min(16, os.cpu_count() or 1))
     lanes, bps, tune = args.served_lanes, 0, None
-    if lanes == 0:  # autotune the launch shape on a sample of the same size distribution
+    if lanes == 0:  # the tuned launch shape for this GPU (cached per GPU model)
         sample = specs[:: max(1, len(specs) // 8)][:8]
-        tune = dlp.autotune([s[0] for s in sample], [s[1] for s in sample], batches=10, max_iterations=300,
-                            device=local_rank)
+        tune = dlp.autotune_cached([s[0] for s in sample], [s[1] for s in sample], batches=10, max_iterations=300,
+                                   device=local_rank)
         lanes, bps = tune["narrow_lanes"], tune["blocks_per_sm"]
-    eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=lanes, blocks_per_sm=bps)
+    eng = dlp.Engine(len(probs), 150 << 30, device=local_rank, narrow_lanes=lanes, blocks_per_sm=bps,
+                     **(tune or {}).get("engine_kw", {}))
     gids = [eng.add_problem(p) for p in probs]
     warm = [p.batches[:skip] for p in probs]  # applied untimed before every measured phase
     for p in probs:  # the requests of this run: batches skip .. skip+nb-1 of each graph
@@ -473,7 +612,6 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     progress(f"batched {batched['value'] / 1e9:.3f} G/s, step max {max(b_ms):.0f} ms")
 
     reqs = [(0.0, g, skip + b, probs[i].batches[b]) for b in range(nb) for i, g in enumerate(gids)]
-
     srv = dlp.Server(eng, memory_budget_bytes=150 << 30, slice_us=args.slice_us)
     for g, p in zip(gids, probs):
         srv.reserve(g, p.batches)
@@ -488,100 +626,174 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
 
     # saturation: everything queued at t = 0
     res, span = replay(reqs)
-    sat_ae = dist_sum(td, sum(r["stats"]["affected_edges"] for r in res))
-    sat_rate = len(res) / span  # this rank's, for its own Poisson trace
+    req_edges = [r["stats"]["affected_edges"] for r in res]
+    total_edges = sum(req_edges)
+    sat_ae = dist_sum(td, total_edges)
+    sat_rate = len(res) / span  # this rank's, for its own Poisson traces
     span = dist_max(td, span)
     svc = [1e3 * (r["finish_s"] - r["admit_s"]) for r in res]
     served_sat = {"value": sat_ae / span, "makespan_s": span, "requests": int(dist_sum(td, len(res))),
                   "requests_per_s": dist_sum(td, sat_rate), "service_ms_p50": dist_max(td, percentile(svc, 0.5)),
                   "service_ms_p99": dist_max(td, percentile(svc, 0.99))}
     progress(f"served saturated {served_sat['value'] / 1e9:.3f} G/s, makespan {span:.1f} s")
-    # Poisson arrivals at half the saturated request rate (each graph's
-    # batches keep their order: arrival k goes to the next request in the list)
-    rng = np.random.default_rng(7)
-    rate = 0.5 * sat_rate
-    times = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
-    trace = [(float(t), g, b, bt) for t, (_, g, b, bt) in zip(times, reqs)]
-    res, span = replay(trace)
+
+    # Poisson sweep: offered rate = fraction x the saturated request rate,
+    # arrivals over a fixed window (a prefix of the batch-major request list)
+    sweep = []
+    for frac in args.poisson_fractions:
+        rate = frac * sat_rate
+        rng = np.random.default_rng(7)
+        times = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+        keep = max(1, int(np.searchsorted(times, args.poisson_window_s, side="right")))
+        trace = [(float(t), g, b, bt) for t, (_, g, b, bt) in zip(times[:keep], reqs[:keep])]
+        res, span = replay(trace)
+        lat = [1e3 * (r["finish_s"] - r["arrival_s"]) for r in res]
+        p_ae = dist_sum(td, sum(r["stats"]["affected_edges"] for r in res))
+        span = dist_max(td, span)
+        row = {"fraction_of_saturated": frac, "offered_requests_per_s": dist_sum(td, rate),
+               "requests": int(dist_sum(td, len(res))), "value": p_ae / span, "makespan_s": span,
+               "latency_ms_p50": dist_max(td, percentile(lat, 0.5)),
+               "latency_ms_p99": dist_max(td, percentile(lat, 0.99)), "latency_ms_max": dist_max(td, max(lat))}
+        sweep.append(row)
+        progress(f"poisson x{frac}: {row['requests']} requests, {row['value'] / 1e9:.3f} G/s, "
+                 f"p50 {row['latency_ms_p50']:.1f} ms, p99 {row['latency_ms_p99']:.1f} ms")
     srv.close()
-    lat = [1e3 * (r["finish_s"] - r["arrival_s"]) for r in res]
-    p_ae = dist_sum(td, sum(r["stats"]["affected_edges"] for r in res))
-    span = dist_max(td, span)
-    served_poisson = {"offered_requests_per_s": dist_sum(td, rate), "value": p_ae / span, "makespan_s": span,
-                      "latency_ms_p50": dist_max(td, percentile(lat, 0.5)),
-                      "latency_ms_p99": dist_max(td, percentile(lat, 0.99)), "latency_ms_max": dist_max(td, max(lat))}
-    progress(f"served poisson {served_poisson['value'] / 1e9:.3f} G/s, p50 {served_poisson['latency_ms_p50']:.1f} ms, "
-             f"p99 {served_poisson['latency_ms_p99']:.1f} ms")
-    # plain: serial, bounded sample — whole graphs (all 10 batches each, in
-    # order) taken in a seeded random order until the time budget is used
+
+    # plain: the same requests, one at a time, graph by graph (stratified sample)
     reset_all()
     srv = dlp.Server(eng, serial=True)
     for g, p in zip(gids, probs):
         srv.reserve(g, p.batches)
-    order = np.random.default_rng(11).permutation(len(gids))
-    graphs_done, pl_ae, pl_t, pl_svc = 0, 0, 0.0, []
-    for i in order:
-        if pl_t >= args.plain_budget_s:
-            break
+    pl_svc, pl_edges, pl_graph_s = [], 0, {}
+
+    def plain_time(i: int) -> float:
+        nonlocal pl_edges
         res, span = srv.replay([(0.0, gids[i], skip + b, probs[i].batches[b]) for b in range(nb)])
-        pl_ae += sum(r["stats"]["affected_edges"] for r in res)
-        pl_t += span
-        pl_svc += [1e3 * (r["finish_s"] - r["admit_s"]) for r in res]
-        graphs_done += 1
+        pl_svc.extend(1e3 * (r["finish_s"] - r["admit_s"]) for r in res)
+        pl_edges += sum(r["stats"]["affected_edges"] for r in res)
+        pl_graph_s[i] = span
+        return span
+    est_s, est_se, sampled = stratified_plain([p.num_nodes for p in probs], plain_time, args.plain_per_stratum,
+                                              args.plain_strata, 11)
     srv.close()
-    plain_v = dist_sum(td, pl_ae / pl_t if pl_t > 0 else 0.0)  # every GPU runs its own plain path
-    progress(f"plain {plain_v / 1e6:.1f} M/s over {graphs_done} graphs")
-    plain = {"value": plain_v, "requests": graphs_done * nb, "seconds": pl_t,
+    plain_v = dist_sum(td, total_edges / est_s if est_s > 0 else 0.0)  # every GPU runs its own plain path
+    lo_v = dist_sum(td, total_edges / (est_s + 2 * est_se) if est_s > 0 else 0.0)
+    hi_v = dist_sum(td, total_edges / max(est_s - 2 * est_se, 1e-9) if est_s > 0 else 0.0)
+    progress(f"plain {plain_v / 1e6:.1f} M/s (estimated {est_s:.1f} +- {est_se:.1f} s for all graphs, "
+             f"{len(sampled)} sampled)")
+    plain = {"value": plain_v, "value_2se_interval": [lo_v, hi_v],
+             "estimated_seconds_all_graphs": est_s, "standard_error_s": est_se,
+             "sampled_graphs": len(sampled), "sampled_requests": len(sampled) * nb,
+             "sampled_seconds": sum(pl_graph_s.values()),
              "service_ms_p50": percentile(pl_svc, 0.5), "service_ms_p99": percentile(pl_svc, 0.99),
-             "sample": f"{graphs_done} of {len(gids)} graphs (seeded random order), all {nb} batches each, "
-                       f"one request at a time"}
+             "sample": (f"stratified: {args.plain_strata} strata by log vertex count, {args.plain_per_stratum} whole "
+                        f"graphs per stratum (seed 11), all {nb} requests of each replayed one at a time; total "
+                        f"time estimated as sum over strata of stratum size x mean graph time; value = the "
+                        f"trace's affected edges / that estimate")}
+    sat_sweep = [r for r in sweep if r["fraction_of_saturated"] == 1.0]
     out = {"workload": (f"mixed-graph stream ({args.served_shape}): {len(all_specs)} graphs ({len(probs)} on this "
                         f"rank of {world}), n log-uniform on [{lo:.0e}, {hi:.0e}], {gen_batches} batches generated per "
                         f"graph, batches {skip}-{skip + nb - 1} served after the first {skip} (numpy seed "
                         f"1000003), degree {{3,5,7}}[i mod 3], generator seed i, batches 90/1/9 insert/GT/delete, "
                         f"delta 1e-4, maxIter 1e5, ref semantics; {vertices} vertices, {edges_full} directed "
-                        f"edges in all"),
+                        f"edges in all; {len(reqs)} requests"),
+           "config": "multi-instance batching (512 graphs)" if args.served_shape == "mixed" and count == 512
+           else f"{count} graphs",
            "setup_s": setup_s, "batched": batched, "served_saturated": served_sat,
-           "served_poisson": served_poisson, "plain": plain,
+           "served_poisson_sweep": sweep, "poisson_window_s": args.poisson_window_s, "plain": plain,
            "served_over_plain": served_sat["value"] / plain_v if plain_v else None,
            "batched_over_plain": batched["value"] / plain_v if plain_v else None,
+           "p99_latency_ms_at_saturated_offer": sat_sweep[0]["latency_ms_p99"] if sat_sweep else None,
            "slice_us": args.slice_us, "narrow_lanes": lanes, "blocks_per_sm": bps or "occupancy",
            "autotune": tune}
     eng.close()
     return out
 
 
+def launch_ranks(argv: list[str], n: int) -> int:
+    """Runs this script as n ranks on this node (one per GPU: RANK, LOCAL_RANK,
+    WORLD_SIZE, MASTER_ADDR/PORT in each one's environment), the way
+    torch.distributed.run would, and waits for all of them. Rank 0 prints the
+    JSON line. Returns the first nonzero exit code, else 0."""
+    import socket
+    with socket.socket() as sk:  # a free port for the gloo rendezvous
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, str(Path(__file__).resolve())] + argv, env=env))
+    codes = [p.wait() for p in procs]
+    return next((c for c in codes if c != 0), 0)
+
+
+def shard_check(args, td, rank, world) -> int:
+    """Host-only check of the multi-rank plumbing (no GPU work): every rank
+    takes its shard of the mixed stream and the per-rank counts are reduced
+    with the same collectives the served block uses."""
+    specs = [(n, d, 10, sd) for n, d, _, sd in mix_sizes(args.served_graphs or 512, 1e3, 5e5, 1000003)]
+    mine = shard_graphs(specs, rank, world)
+    load = sum(specs[i][0] * specs[i][1] for i in mine)
+    graphs = int(dist_sum(td, len(mine)))
+    total_load = int(dist_sum(td, load))
+    max_load = int(dist_max(td, load))
+    if td is not None:
+        import torch
+        t = torch.zeros(len(specs), dtype=torch.int64)
+        t[mine] = rank + 1
+        td.all_reduce(t)
+        owners = t.tolist()
+    else:
+        owners = [1] * len(specs)
+    if rank == 0:
+        print(json.dumps({"impl": "shard-check", "n_gpus": world, "graphs": graphs, "total_load": total_load,
+                          "max_load": max_load, "owners": owners}), flush=True)
+    return 0
+
+
 def main(argv=None) -> int:
+    argv = list(sys.argv[1:] if argv is None else argv)
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--impl", choices=["gb300", "reference", "shard-check"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="config2")
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--batches", type=int, default=0, help="replay only the first N batches (0: all)")
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--ref-budget-s", type=float, default=20.0)
-    ap.add_argument("--served-graphs", type=int, default=64)
+    ap.add_argument("--served-graphs", type=int, default=0, help="0: 512 (mixed shape) / 256 (stream shape)")
     ap.add_argument("--served-shape", choices=["mixed", "stream"], default="mixed",
                     help="mixed: sizes 1e3-5e5, 10 batches; stream: sizes 1e4-5e6, 40 batches (about 2%% of a graph "
                          "per request), the first --served-batches of each served")
     ap.add_argument("--served-batches", type=int, default=5)
     ap.add_argument("--served-skip", type=int, default=-1, help="stream shape: batches applied before serving "
                     "(default 20)")
-    ap.add_argument("--served-lanes", type=int, default=0, help="0: autotune")
+    ap.add_argument("--served-lanes", type=int, default=0, help="0: the tuned shape")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--slice-us", type=float, default=2000.0)
-    ap.add_argument("--plain-budget-s", type=float, default=20.0)
+    ap.add_argument("--poisson-fractions", type=lambda x: [float(v) for v in x.split(",")],
+                    default=[0.25, 0.5, 0.75, 1.0], help="offered rates as fractions of the saturated rate")
+    ap.add_argument("--poisson-window-s", type=float, default=15.0, help="arrival window of each Poisson run")
+    ap.add_argument("--plain-per-stratum", type=int, default=3)
+    ap.add_argument("--plain-strata", type=int, default=8)
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip timing the reference's own CUDA build (oracle/_ref/ref_kernels)")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        return launch_ranks(argv, args.gpus)
     rank, world, local_rank = dist_env()
     td = dist_init(world)
     try:
         if args.impl == "reference":
             return reference_arm(args, td, rank)
+        if args.impl == "shard-check":
+            return shard_check(args, td, rank, world)
         from labelpropcuda_gb300 import build
         build.build()
         return gpu_arm(args, td, rank, world, local_rank)

@@ -229,6 +229,12 @@ int dlp_engine_restore(dlp_engine *e, const void *snapshot, size_t bytes, int *g
 /* Same, into the given free graph id (so a graph can keep its id across an
  * eviction). */
 int dlp_engine_restore_as(dlp_engine *e, const void *snapshot, size_t bytes, int graph_id);
+/* Keeps a free graph id for a graph that was removed to host memory:
+ * dlp_engine_add_graph and dlp_engine_restore skip a held id, and
+ * dlp_engine_restore_as into it releases the hold. Release without a restore
+ * with dlp_engine_release_id. No counterpart in the reference. */
+int dlp_engine_hold_id(dlp_engine *e, int graph_id);
+int dlp_engine_release_id(dlp_engine *e, int graph_id);
 /* Device bytes a resident graph occupies (0 for an unknown id). */
 size_t dlp_engine_graph_resident_bytes(const dlp_engine *e, int graph_id);
 int dlp_engine_reset_graph(dlp_engine *e, int graph_id);
@@ -441,6 +447,8 @@ int dlp_irlp(const int *d_row_ptr, const int *d_col_ind, const float *d_values, 
 /* Device helpers for bindings that have no CUDA runtime of their own.       */
 /* ------------------------------------------------------------------------ */
 int dlp_device_count(int *count);
+/* "<name> sm_<major><minor> <SMs> SMs" of a device (the autotuner's cache key). */
+int dlp_device_name(int device, char *out, int capacity);
 int dlp_set_device(int device);
 int dlp_malloc(void **ptr, size_t bytes);
 int dlp_free(void *ptr);

@@ -379,6 +379,56 @@ def autotune(sizes: list[int], degrees: list[int], batches: int = 10, max_iterat
     return {"narrow_lanes": cfg.narrow_lanes, "blocks_per_sm": cfg.blocks_per_sm, "candidates": cands}
 
 
+def device_name(device: int = 0) -> str:
+    buf = ctypes.create_string_buffer(256)
+    _n.check(_n.lib().dlp_device_name(device, buf, 256))
+    return buf.value.decode()
+
+
+def _kernel_digest() -> str:
+    """Digest of the engine kernel's sources: a tuned shape is only reused for
+    the kernel it was measured on."""
+    import hashlib
+    from pathlib import Path
+    h = hashlib.sha256()
+    for name in ("engine_kernel.cu", "engine.cuh", "row_sums.cuh", "session_kernel.cuh", "tune.cu"):
+        f = Path(__file__).resolve().parent / "csrc" / name
+        if f.exists():
+            h.update(f.read_bytes())
+    return h.hexdigest()[:16]
+
+
+def autotune_cached(sizes: list[int], degrees: list[int], batches: int = 10, max_iterations: int = 2000,
+                    cache_path: str | None = None, **config) -> dict:
+    """autotune() with a JSON cache keyed by GPU model and engine-kernel
+    digest (DLP_TUNE_CACHE, default ~/.cache/dlp_gb300/tune.json): a GPU model
+    is tuned once per kernel version and the choice is reused after that.
+    The result says where it came from ("source": "cache" or "measured")."""
+    import json
+    import os
+    from pathlib import Path
+    path = Path(cache_path or os.environ.get("DLP_TUNE_CACHE") or
+                Path.home() / ".cache" / "dlp_gb300" / "tune.json")
+    key = f"{device_name(config.get('device', 0))} | kernel {_kernel_digest()} | " \
+          f"sizes {sorted(sizes)} degrees {sorted(degrees)} batches {batches} max_iter {max_iterations}"
+    try:
+        cache = json.loads(path.read_text())
+    except (OSError, ValueError):
+        cache = {}
+    if key in cache:
+        return dict(cache[key], source="cache", key=key)
+    r = autotune(sizes, degrees, batches=batches, max_iterations=max_iterations, **config)
+    cache[key] = r
+    try:
+        path.parent.mkdir(parents=True, exist_ok=True)
+        tmp = path.with_suffix(".tmp")
+        tmp.write_text(json.dumps(cache, indent=1))
+        tmp.replace(path)
+    except OSError:
+        pass
+    return dict(r, source="measured", key=key)
+
+
 class Server:
     """Continuous batching over an Engine (dlp_server_*): requests wait in
     arrival order; each poll admits what fits and runs one sliced step over the

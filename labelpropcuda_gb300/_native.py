@@ -163,6 +163,8 @@ _SIGNATURES = {
     "dlp_engine_restore": (_I, [_P, _P, ctypes.c_size_t, c_int_p]),
     "dlp_engine_restore_as": (_I, [_P, _P, ctypes.c_size_t, _I]),
     "dlp_engine_graph_resident_bytes": (ctypes.c_size_t, [_P, _I]),
+    "dlp_engine_hold_id": (_I, [_P, _I]),
+    "dlp_engine_release_id": (_I, [_P, _I]),
     "dlp_server_evictions": (_I, [_P, c_int_p, c_int_p]),
     "dlp_server_make_resident": (_I, [_P, _I]),
     "dlp_autotune": (_I, [ctypes.POINTER(Config), _I, c_int_p, c_int_p, _I, _I, ctypes.POINTER(TuneReport)]),
@@ -188,6 +190,7 @@ _SIGNATURES = {
     "dlp_iterative_propagation_noalloc": (_I, [_P, _P, _P, _P, _P, _P, _P, _P, _I, ctypes.c_float, _I, c_int_p,
                                                _P]),
     "dlp_device_count": (_I, [c_int_p]),
+    "dlp_device_name": (_I, [_I, ctypes.c_char_p, _I]),
     "dlp_set_device": (_I, [_I]),
     "dlp_malloc": (_I, [ctypes.POINTER(_P), ctypes.c_size_t]),
     "dlp_free": (_I, [_P]),

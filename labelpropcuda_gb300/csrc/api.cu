@@ -1,5 +1,6 @@
 // C ABI plumbing: error reporting, device checks, the problem (input
 // generation) object and small device helpers for bindings.
+#include <cstdio>
 #include <cstring>
 #include <string>
 
@@ -156,6 +157,15 @@ int dlp_device_count(int *count) {
     cudaGetLastError();
     *count = 0;
   }
+  return DLP_OK;
+}
+int dlp_device_name(int device, char *out, int capacity) {
+  dlp::clear_error();
+  if (!out || capacity <= 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null name buffer");
+  cudaDeviceProp prop;
+  DLP_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  std::snprintf(out, static_cast<size_t>(capacity), "%s sm_%d%d %d SMs", prop.name, prop.major, prop.minor,
+                prop.multiProcessorCount);
   return DLP_OK;
 }
 int dlp_set_device(int device) {

@@ -150,6 +150,7 @@ struct dlp_engine {
   char *stage_dev[2] = {nullptr, nullptr};
   size_t stage_cap[2] = {0, 0};
   std::vector<GraphSlot *> graphs;  // by graph id (nullptr: free id)
+  std::vector<char> held;           // by graph id: a free id kept for a graph evicted to host memory
   int steps = 0;
   cudaEvent_t ev[kStepRing][2];
   bool ev_made = false;
@@ -629,6 +630,7 @@ int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_bu
       cudaMemset(e->bc_all, 0, sizeof(BatchCounters) * max_graphs) != cudaSuccess)
     return bail(dlp::fail(DLP_ERR_CUDA, "initialisation failed"));
   e->graphs.assign(max_graphs, nullptr);
+  e->held.assign(max_graphs, 0);
   *out = e;
   return DLP_OK;
 }
@@ -665,7 +667,7 @@ int dlp_engine_add_graph(dlp_engine *e, int n, int64_t m, const int *row_ptr, co
                                                 " bytes)");
   int gid = -1;
   for (int i = 0; i < e->max_graphs; ++i)
-    if (!e->graphs[i]) {
+    if (!e->graphs[i] && !e->held[i]) {
       gid = i;
       break;
     }
@@ -827,7 +829,7 @@ int restore_graph(dlp_engine *e, const void *snapshot, size_t bytes, int want, i
     gid = want;
   } else {
     for (int i = 0; i < e->max_graphs; ++i)
-      if (!e->graphs[i]) {
+      if (!e->graphs[i] && !e->held[i]) {
         gid = i;
         break;
       }
@@ -874,6 +876,7 @@ int restore_graph(dlp_engine *e, const void *snapshot, size_t bytes, int want, i
   g->seq_batch.assign(reinterpret_cast<const int *>(p), reinterpret_cast<const int *>(p) + h.seq);
   g->seq_step.assign(h.seq, -1);
   e->graphs[gid] = g;
+  e->held[gid] = 0;
   e->used += g->bytes;
   *graph_id = gid;
   return DLP_OK;
@@ -891,6 +894,21 @@ int dlp_engine_restore_as(dlp_engine *e, const void *snapshot, size_t bytes, int
   if (!e || !snapshot || graph_id < 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument or negative id");
   int got = -1;
   return restore_graph(e, snapshot, bytes, graph_id, &got);
+}
+
+int dlp_engine_hold_id(dlp_engine *e, int graph_id) {
+  dlp::clear_error();
+  if (!e || graph_id < 0 || graph_id >= e->max_graphs) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "bad graph id");
+  if (e->graphs[graph_id]) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "graph id is in use");
+  e->held[graph_id] = 1;
+  return DLP_OK;
+}
+
+int dlp_engine_release_id(dlp_engine *e, int graph_id) {
+  dlp::clear_error();
+  if (!e || graph_id < 0 || graph_id >= e->max_graphs) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "bad graph id");
+  e->held[graph_id] = 0;
+  return DLP_OK;
 }
 
 size_t dlp_engine_graph_resident_bytes(const dlp_engine *e, int graph_id) {

@@ -64,8 +64,8 @@ struct Request {
   int batch = 0;
   dlp_batch_view host{};
   std::unique_ptr<HostBatch> owned;
-  size_t batch_bytes = 0;  // the arrays on the device
-  size_t bytes = 0;        // batch_bytes + the engine's edge / deletion scratch
+  size_t batch_bytes = 0;  // the arrays on the device (in its graph's staging buffer)
+  size_t bytes = 0;        // the engine's edge / deletion scratch the batch needs
   bool done = false;
   dlp_request_result res{};
 };
@@ -83,6 +83,7 @@ struct GraphBuf {
   size_t graph_bytes = 0;  // its device bytes when resident
   int nodes = 0;
   double last_use = 0.0;
+  int res_edges = 0, res_deleted = 0;  // engine scratch reserved by dlp_server_reserve
 };
 
 size_t batch_bytes(const dlp_batch_view &v) {
@@ -117,20 +118,26 @@ struct dlp_server {
   Clock::time_point t0;
   std::vector<Request> reqs;
   std::deque<int> queue;
-  std::vector<GraphBuf> bufs;
+  // One entry per possible graph id, sized once at creation: a reference into
+  // it stays valid for the server's lifetime.
+  std::vector<GraphBuf> bufs = std::vector<GraphBuf>(dlp::engine::kMaxGraphs);
   size_t running_bytes = 0;
+  size_t staged_bytes = 0;  // device bytes of every graph's staging buffer
   int running = 0;
   int evictions = 0, restores = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
-  GraphBuf &buf(int gid) {
-    if (gid >= static_cast<int>(bufs.size())) bufs.resize(gid + 1);
-    return bufs[gid];
-  }
+  // gid must be a valid graph id (graph_nodes(gid) > 0).
+  GraphBuf &buf(int gid) { return bufs[gid]; }
 
+  // Graphs still evicted go back into the engine (best effort: a graph that
+  // no longer fits is dropped and its id released).
   ~dlp_server() {
-    for (GraphBuf &b : bufs) {
+    for (size_t gid = 0; gid < bufs.size(); ++gid) {
+      GraphBuf &b = bufs[gid];
+      if (b.evicted && dlp_engine_restore_as(eng, b.snap.data(), b.snap.size(), static_cast<int>(gid)) != DLP_OK)
+        dlp_engine_release_id(eng, static_cast<int>(gid));
       if (b.dev) cudaFree(b.dev);
       if (b.pinned) cudaFreeHost(b.pinned);
     }
@@ -144,8 +151,16 @@ struct dlp_server {
     return -1;
   }
 
+  void free_staging(GraphBuf &b) {
+    if (b.dev) cudaFree(b.dev);
+    staged_bytes -= std::min(staged_bytes, b.dev_cap);
+    b.dev = nullptr;
+    b.dev_cap = 0;
+  }
+
   // Evicts graph gid: its whole device state to host memory, then its device
-  // memory freed. Only for a graph with no batch in progress.
+  // memory (graph and staging buffer) freed. Its id stays held in the engine,
+  // so no other graph can take it. Only for a graph with no batch in progress.
   int evict(int gid) {
     GraphBuf &b = buf(gid);
     size_t bytes = 0;
@@ -155,11 +170,16 @@ struct dlp_server {
     b.graph_bytes = dlp_engine_graph_resident_bytes(eng, gid);
     b.nodes = dlp_engine_graph_nodes(eng, gid);
     DLP_TRY(dlp_engine_remove_graph(eng, gid));
+    DLP_TRY(dlp_engine_hold_id(eng, gid));
+    DLP_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(dlp_engine_stream(eng))));
+    free_staging(b);
     b.evicted = true;
     ++evictions;
     return DLP_OK;
   }
 
+  // Makes an evicted graph resident again under its id. This allocates its
+  // device memory again, and its reserved engine scratch.
   int restore(int gid) {
     GraphBuf &b = buf(gid);
     DLP_TRY(dlp_engine_restore_as(eng, b.snap.data(), b.snap.size(), gid));
@@ -167,13 +187,22 @@ struct dlp_server {
     b.snap.shrink_to_fit();
     b.evicted = false;
     ++restores;
+    if (b.res_edges > 0 || b.res_deleted > 0) DLP_TRY(dlp_engine_reserve(eng, gid, b.res_edges, b.res_deleted));
     return DLP_OK;
   }
 
-  // Bytes the budget counts: resident graphs plus running requests.
+  // Bytes the budget counts: resident graphs, every staging buffer, and the
+  // engine scratch of running requests.
   bool fits(size_t need) const {
     return cfg.memory_budget_bytes == 0 ||
-           dlp_engine_bytes_in_use(eng) + running_bytes + need <= cfg.memory_budget_bytes;
+           dlp_engine_bytes_in_use(eng) + staged_bytes + running_bytes + need <= cfg.memory_budget_bytes;
+  }
+
+  // Staging bytes a request adds to its graph's buffer (grow() keeps twice
+  // what it is asked for).
+  static size_t staging_growth(const GraphBuf &b, const Request &r) {
+    const size_t total = std::max<size_t>(r.batch_bytes, 16);
+    return total > b.dev_cap ? 2 * total - b.dev_cap : 0;
   }
 
   // Evicts idle resident graphs, least recently used first (never `keep` nor
@@ -182,15 +211,11 @@ struct dlp_server {
     *ok = fits(need);
     while (!*ok && cfg.evict_idle) {
       int victim = -1;
-      for (int g = 0; g < dlp::engine::kMaxGraphs; ++g) {
+      for (int g = 0; g < static_cast<int>(bufs.size()); ++g) {
         if (g == keep || dlp_engine_graph_nodes(eng, g) <= 0) continue;
-        if (g < static_cast<int>(bufs.size()) && bufs[g].running >= 0) continue;
+        if (bufs[g].running >= 0) continue;
         if (std::find(busy.begin(), busy.end(), g) != busy.end()) continue;
-        const double lu = g < static_cast<int>(bufs.size()) ? bufs[g].last_use : 0.0;
-        if (victim < 0 || lu < bufs[victim].last_use) {
-          buf(g);  // the victim needs an entry for its snapshot
-          victim = g;
-        }
+        if (victim < 0 || bufs[g].last_use < bufs[victim].last_use) victim = g;
       }
       if (victim < 0) break;
       DLP_TRY(evict(victim));
@@ -211,7 +236,7 @@ struct dlp_server {
       q.host = r.batch;
     }
     q.batch_bytes = batch_bytes(q.host);
-    q.bytes = q.batch_bytes + 24 * static_cast<size_t>(q.host.num_edges) + 8 * static_cast<size_t>(q.host.num_deleted);
+    q.bytes = 24 * static_cast<size_t>(q.host.num_edges) + 8 * static_cast<size_t>(q.host.num_deleted);
     q.res.graph_id = r.graph_id;
     q.res.batch_index = r.batch_index;
     q.res.status = DLP_OK;
@@ -236,11 +261,10 @@ struct dlp_server {
     }
     if (total > b.dev_cap) {
       DLP_CUDA_TRY(cudaStreamSynchronize(s));
-      if (b.dev) cudaFree(b.dev);
-      b.dev = nullptr;
-      b.dev_cap = 0;
+      free_staging(b);
       DLP_CUDA_TRY(cudaMalloc(&b.dev, total * 2));
       b.dev_cap = total * 2;
+      staged_bytes += b.dev_cap;
     }
     return DLP_OK;
   }
@@ -299,7 +323,7 @@ struct dlp_server {
     for (auto it = queue.begin(); it != queue.end() && static_cast<int>(gids.size()) < limit;) {
       Request &r = reqs[*it];
       if (r.gid >= static_cast<int>(blocked.size())) blocked.resize(r.gid + 1, 0);
-      GraphBuf &b = buf(r.gid);
+      GraphBuf &b = buf(r.gid);  // bufs never reallocates, so b stays valid across make_room
       // one batch per graph at a time, in arrival order
       if (b.running >= 0 || blocked[r.gid]) {
         blocked[r.gid] = 1;
@@ -307,7 +331,7 @@ struct dlp_server {
         continue;
       }
       // an evicted graph needs its own bytes back as well
-      const size_t need = r.bytes + (b.evicted ? b.graph_bytes : 0);
+      const size_t need = r.bytes + staging_growth(b, r) + (b.evicted ? b.graph_bytes : 0);
       bool ok = true;
       DLP_TRY(make_room(need, r.gid, gids, &ok));
       if (!ok) {
@@ -430,14 +454,18 @@ int dlp_server_reserve(dlp_server *s, int graph_id, int max_inserted, int max_gt
   dlp::clear_error();
   if (!s || max_inserted < 0 || max_gt < 0 || max_deleted < 0 || max_edges < 0)
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null server or negative size");
-  if (dlp_engine_graph_nodes(s->eng, graph_id) <= 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph id");
+  if (s->graph_nodes(graph_id) <= 0) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "unknown graph id");
   dlp_batch_view v{};
   v.num_inserted = max_inserted;
   v.num_gt = max_gt;
   v.num_deleted = max_deleted;
   v.num_edges = max_edges;
   const size_t total = std::max<size_t>(batch_bytes(v), 16);
-  DLP_TRY(s->grow(s->buf(graph_id), (total + 1) / 2));  // grow() keeps twice what it is asked for
+  GraphBuf &b = s->buf(graph_id);
+  b.res_edges = std::max(b.res_edges, max_edges);
+  b.res_deleted = std::max(b.res_deleted, max_deleted);
+  if (b.evicted) return DLP_OK;  // applied when the graph is restored
+  DLP_TRY(s->grow(b, (total + 1) / 2));  // grow() keeps twice what it is asked for
   return dlp_engine_reserve(s->eng, graph_id, max_edges, max_deleted);
 }
 

@@ -48,6 +48,10 @@ struct orc_run {
   std::vector<int8_t> status;  // host-side status (what the reference keeps on the host)
   std::vector<int8_t> gt;      // -1 / 0 / 1
   std::vector<float> labels;
+  int fp64 = 0;                 // 1: labels and propagation arithmetic in double;
+                                // 2: fp32 run plus a double shadow of each batch's propagation
+  std::vector<double> lab64;    // the labels in FP64 mode / the shadow's result
+  int shadow_iterations = 0;
   std::string err;
 
   // scratch
@@ -130,6 +134,81 @@ struct DSU {
   }
 };
 
+// Frontier propagation (src/iterativePropagation.cu:241-346) over `labels`
+// (float: the reference's arithmetic; double: the FP64 oracle). Two buffers
+// that both start at the initial labels; pass k reads buffer k%2 and writes
+// buffer (k+1)%2 at frontier vertices only; the result is buffer (passes % 2).
+template <class T>
+void propagate(orc_run *r, std::vector<T> &labels, std::vector<int> frontier, orc_stats &st,
+               std::vector<int> &sizes) {
+  std::vector<T> buf[2] = {labels, labels};
+  const int T_ = nthreads(r);
+  std::vector<std::vector<int>> marks_t(T_);
+  auto skip = [&](int v) { return v < 0 || r->dev_status[v] == kDeleted; };
+  int passes = 0;
+  for (int k = 0; k < r->max_iter; ++k) {
+    if (frontier.empty()) break;
+    sizes.push_back(static_cast<int>(frontier.size()));
+    const T *src = buf[k & 1].data();
+    T *dst = buf[(k + 1) & 1].data();
+    int64_t edges = 0;
+    const int F = static_cast<int>(frontier.size());
+#pragma omp parallel num_threads(T_) reduction(+ : edges)
+    {
+      std::vector<int> &mine = marks_t[omp_get_thread_num()];
+      mine.clear();
+#pragma omp for schedule(static)
+      for (int i = 0; i < F; ++i) {
+        const int u = frontier[i];
+        const int s = r->arp[u], len = r->arp[u + 1] - s;
+        edges += len;
+        T nl, old = src[u];
+        if constexpr (sizeof(T) == sizeof(float)) {
+          float wa, wl;
+          orc::row_sums(&r->acol[s], &r->aval[s], len, src, skip, wa, wl);
+          nl = orc::updated_label(wa, wl, old);
+        } else {
+          double wa, wl;
+          orc::row_sums64(&r->acol[s], &r->aval[s], len, src, skip, wa, wl);
+          nl = orc::updated_label64(wa, wl, old);
+        }
+        dst[u] = nl;
+        if (std::fabs(nl - old) > static_cast<T>(r->delta)) {
+          // Mark non-deleted, non-ground-truth neighbours and u itself
+          // (src/iterativePropagation.cu:187-217).
+          for (int e = s; e < s + len; ++e) {
+            const int v = r->acol[e];
+            if (v >= 0 && r->dev_status[v] != kDeleted && r->gt[v] < 0) mine.push_back(v);
+          }
+          if (r->gt[u] < 0) mine.push_back(u);
+        }
+      }
+    }
+    st.affected_edges += edges;
+    st.frontier_visits += F;
+    passes = k + 1;
+    // Next frontier: marked, active and not ground truth.
+    ++r->stamp_clock;
+    std::vector<int> next;
+    for (int t = 0; t < T_; ++t)
+      for (int v : marks_t[t])
+        if (r->stamp[v] != r->stamp_clock) {
+          r->stamp[v] = r->stamp_clock;
+          if (r->dev_status[v] == kActive && r->gt[v] < 0) next.push_back(v);
+        }
+    std::sort(next.begin(), next.end());
+    frontier.swap(next);
+    // A pass with no change marks nothing, so an empty next frontier is the
+    // reference's "nothing changed" exit as well.
+  }
+  st.iterations = passes;
+  labels = buf[passes & 1];
+  for (size_t v = 0; v < labels.size(); ++v) {  // src/iterativePropagation.cu:224-235
+    if (r->gt[v] == 0) labels[v] = 0;
+    else if (r->gt[v] == 1) labels[v] = 1;
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -178,6 +257,15 @@ void orc_destroy(orc_run *r) { delete r; }
 float orc_tau(const orc_run *r) { return r->tau; }
 const char *orc_error(const orc_run *r) { return r->err.c_str(); }
 const float *orc_labels(const orc_run *r) { return r->labels.data(); }
+const double *orc_labels64(const orc_run *r) { return r->fp64 ? r->lab64.data() : nullptr; }
+int orc_shadow_iterations(const orc_run *r) { return r->shadow_iterations; }
+
+int orc_set_fp64(orc_run *r, int mode) {
+  if (!r || mode < 0 || mode > 2) return 1;
+  r->fp64 = mode;
+  r->lab64.assign(r->labels.begin(), r->labels.end());
+  return 0;
+}
 
 const void *orc_artefact(const orc_run *r, int which, int64_t *count) {
   if (which < 0 || which >= ORC_ART_COUNT || !r->record) {
@@ -218,6 +306,7 @@ int orc_apply_batch(orc_run *r, int b, const orc_batch_in *in, orc_stats *out) {
     const int v = in->gt_ids[i];
     r->gt[v] = in->gt_labels[i] < 0.5f ? 0 : 1;
     r->labels[v] = in->gt_labels[i];
+    if (r->fp64) r->lab64[v] = in->gt_labels[i];
   }
 
   // ---- host status update ----
@@ -412,6 +501,16 @@ int orc_apply_batch(orc_run *r, int b, const orc_batch_in *in, orc_stats *out) {
         l = den > 1e-10f ? c / den : 0.5f;
       }
       r->labels[u] = l;
+      if (r->fp64) {
+        double l64 = l;
+        if (r->gt[u] < 0 && comp_id[i] >= 0) {
+          const double a = static_cast<double>(w0[comp_id[i]]) * (1.0 / 4294967296.0);
+          const double c = static_cast<double>(w1[comp_id[i]]) * (1.0 / 4294967296.0);
+          const double den = a + c;
+          l64 = den > 1e-10 ? c / den : 0.5;
+        }
+        r->lab64[u] = l64;
+      }
     }
   } else if (I > 0) {
     // New vertices without new edges (src/dynLP.cu:482-504): ground truth
@@ -426,6 +525,7 @@ int orc_apply_batch(orc_run *r, int b, const orc_batch_in *in, orc_stats *out) {
         for (const auto &p : batch_gt)
           if (p.first == v) l = p.second;
       r->labels[v] = l;
+      if (r->fp64) r->lab64[v] = l;
     }
   }
   if (r->record) {
@@ -442,10 +542,6 @@ int orc_apply_batch(orc_run *r, int b, const orc_batch_in *in, orc_stats *out) {
   }
 
   // ---- step 3: frontier propagation (src/iterativePropagation.cu:241-346) ----
-  // Two buffers that both start at the initial labels; pass k reads buffer
-  // k%2 and writes buffer (k+1)%2 at frontier vertices only; the result is
-  // buffer (passes % 2).
-  std::vector<float> buf[2] = {r->labels, r->labels};
   std::vector<int> frontier;
   for (int v = 0; v < n; ++v) {
     if (r->affected[v]) ++st.seed_marks;
@@ -454,64 +550,20 @@ int orc_apply_batch(orc_run *r, int b, const orc_batch_in *in, orc_stats *out) {
   st.seed_frontier = static_cast<int>(frontier.size());
   set_art(r, ORC_ART_FRONTIER0, frontier);
   std::vector<int> sizes;
-  const int T = nthreads(r);
-  std::vector<std::vector<int>> marks_t(T);
-  auto skip = [&](int v) { return v < 0 || r->dev_status[v] == kDeleted; };
-  int passes = 0;
-  for (int k = 0; k < r->max_iter; ++k) {
-    if (frontier.empty()) break;
-    sizes.push_back(static_cast<int>(frontier.size()));
-    const float *src = buf[k & 1].data();
-    float *dst = buf[(k + 1) & 1].data();
-    int64_t edges = 0;
-    const int F = static_cast<int>(frontier.size());
-#pragma omp parallel num_threads(T) reduction(+ : edges)
-    {
-      std::vector<int> &mine = marks_t[omp_get_thread_num()];
-      mine.clear();
-#pragma omp for schedule(static)
-      for (int i = 0; i < F; ++i) {
-        const int u = frontier[i];
-        const int s = r->arp[u], len = r->arp[u + 1] - s;
-        edges += len;
-        float wa, wl;
-        orc::row_sums(&r->acol[s], &r->aval[s], len, src, skip, wa, wl);
-        const float old = src[u];
-        const float nl = orc::updated_label(wa, wl, old);
-        dst[u] = nl;
-        if (std::fabs(nl - old) > r->delta) {
-          // Mark non-deleted, non-ground-truth neighbours and u itself
-          // (src/iterativePropagation.cu:187-217).
-          for (int e = s; e < s + len; ++e) {
-            const int v = r->acol[e];
-            if (v >= 0 && r->dev_status[v] != kDeleted && r->gt[v] < 0) mine.push_back(v);
-          }
-          if (r->gt[u] < 0) mine.push_back(u);
-        }
-      }
+  if (r->fp64 == 1) {
+    propagate(r, r->lab64, std::move(frontier), st, sizes);
+    for (int v = 0; v < n; ++v) r->labels[v] = static_cast<float>(r->lab64[v]);
+  } else {
+    if (r->fp64 == 2) {
+      // the same batch's propagation in double, from the same state
+      r->lab64.assign(r->labels.begin(), r->labels.end());
+      orc_stats sh;
+      std::memset(&sh, 0, sizeof(sh));
+      std::vector<int> sh_sizes;
+      propagate(r, r->lab64, frontier, sh, sh_sizes);
+      r->shadow_iterations = sh.iterations;
     }
-    st.affected_edges += edges;
-    st.frontier_visits += F;
-    passes = k + 1;
-    // Next frontier: marked, active and not ground truth.
-    ++r->stamp_clock;
-    std::vector<int> next;
-    for (int t = 0; t < T; ++t)
-      for (int v : marks_t[t])
-        if (r->stamp[v] != r->stamp_clock) {
-          r->stamp[v] = r->stamp_clock;
-          if (r->dev_status[v] == kActive && r->gt[v] < 0) next.push_back(v);
-        }
-    std::sort(next.begin(), next.end());
-    frontier.swap(next);
-    // A pass with no change marks nothing, so an empty next frontier is the
-    // reference's "nothing changed" exit as well.
-  }
-  st.iterations = passes;
-  r->labels = buf[passes & 1];
-  for (int v = 0; v < n; ++v) {  // src/iterativePropagation.cu:224-235
-    if (r->gt[v] == 0) r->labels[v] = 0.0f;
-    else if (r->gt[v] == 1) r->labels[v] = 1.0f;
+    propagate(r, r->labels, std::move(frontier), st, sizes);
   }
   set_art(r, ORC_ART_FRONTIER_SIZES, sizes);
   set_art(r, ORC_ART_LABELS, r->labels);

@@ -92,6 +92,19 @@ orc_run *orc_create(int n, const int *row_ptr, const int *col_ind,
                     int max_iterations, int semantics, int threads, int record);
 void orc_destroy(orc_run *r);
 float orc_tau(const orc_run *r);
+/* FP64 modes (set before the first batch).
+ * mode 1: the same schedule with every label and every propagation /
+ *   initialisation product, sum and quotient in double; orc_labels returns
+ *   the double labels rounded to float, orc_labels64 the double labels.
+ * mode 2 (shadow): the fp32 run as usual, plus each batch's propagation
+ *   repeated in double from the same state (labels after initialisation, the
+ *   same first frontier); orc_labels64 returns the shadow's labels after the
+ *   batch and orc_shadow_iterations its pass count. This isolates one batch's
+ *   fp32 error from the drift of earlier batches.
+ * orc_labels64 is NULL in mode 0. */
+int orc_set_fp64(orc_run *r, int mode);
+const double *orc_labels64(const orc_run *r);
+int orc_shadow_iterations(const orc_run *r);
 /* Returns 0 on success, nonzero on invalid input (message in orc_error). */
 int orc_apply_batch(orc_run *r, int batch_index, const orc_batch_in *in,
                     orc_stats *out);
@@ -105,6 +118,22 @@ const void *orc_artefact(const orc_run *r, int which, int64_t *count);
 int orc_irlp(int n, const int *row_ptr, const int *col_ind, const float *values,
              const int *status, const int *gt_class, float *labels, float delta,
              int max_iterations, int threads, int64_t *edge_visits);
+
+/* The reference's input generator, restated (generate_oracle.cpp): full
+ * graph, true labels and batches for the given arguments. The batch views
+ * point into the problem and stay valid until orc_problem_free. */
+typedef struct orc_problem orc_problem;
+orc_problem *orc_generate(int n, int avg_degree, int num_batches, unsigned seed,
+                          float gt_fraction, float deleted_fraction);
+void orc_problem_free(orc_problem *p);
+int orc_problem_num_nodes(const orc_problem *p);
+int64_t orc_problem_num_edges(const orc_problem *p);
+const int *orc_problem_row_ptr(const orc_problem *p);
+const int *orc_problem_col_ind(const orc_problem *p);
+const float *orc_problem_values(const orc_problem *p);
+const float *orc_problem_true_labels(const orc_problem *p);
+int orc_problem_num_batches(const orc_problem *p);
+int orc_problem_batch(const orc_problem *p, int b, orc_batch_in *out);
 
 #ifdef __cplusplus
 }

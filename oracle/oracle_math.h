@@ -41,6 +41,30 @@ inline void row_sums(const int *col, const float *val, int len, const float *lab
   w_label = sl[0];
 }
 
+// The same order in double precision throughout (the FP64 oracle: the same
+// schedule with every label, product and sum in double).
+template <class Skip>
+inline void row_sums64(const int *col, const float *val, int len, const double *labels,
+                       Skip skip, double &w_all, double &w_label) {
+  const int slots = len <= 32 ? 32 : 256;
+  double sw[256], sl[256];
+  for (int s = 0; s < slots; ++s) sw[s] = sl[s] = 0.0;
+  for (int e = 0; e < len; ++e) {
+    const int v = col[e];
+    if (skip(v)) continue;
+    const int s = e & 255;
+    sw[s] = sw[s] + static_cast<double>(val[e]);
+    sl[s] = std::fma(static_cast<double>(val[e]), labels[v], sl[s]);
+  }
+  for (int stride = slots / 2; stride > 0; stride >>= 1)
+    for (int t = 0; t < stride; ++t) {
+      sw[t] = sw[t] + sw[t + stride];
+      sl[t] = sl[t] + sl[t + stride];
+    }
+  w_all = sw[0];
+  w_label = sl[0];
+}
+
 // New label from the two sums (src/iterativePropagation.cu:153-168): keep the
 // old label when the weight sum is not above 1e-10, clamp to [0, 1]. The
 // division is IEEE round-to-nearest (the reference's --use_fast_math build uses
@@ -48,6 +72,11 @@ inline void row_sums(const int *col, const float *val, int len, const float *lab
 inline float updated_label(float w_all, float w_label, float old) {
   float nl = (w_all > 1e-10f) ? (w_label / w_all) : old;
   return std::fmin(std::fmax(nl, 0.0f), 1.0f);
+}
+
+inline double updated_label64(double w_all, double w_label, double old) {
+  double nl = (w_all > 1e-10) ? (w_label / w_all) : old;
+  return std::fmin(std::fmax(nl, 0.0), 1.0);
 }
 
 // Supernode weights are summed exactly in 32.32 fixed point, so the sum does

@@ -253,3 +253,28 @@ def test_server_evicts_idle_graphs_to_fit_the_budget(gpu):
         srv.make_resident(gid)
         assert eng.labels(gid).tobytes() == want[i][-1][1].tobytes()
     srv.close()
+
+
+@pytest.mark.gpu
+def test_evicted_graph_keeps_its_id(gpu):
+    """A graph evicted by the server keeps its id: a graph added to the engine
+    meanwhile takes another id, and the evicted one comes back intact."""
+    p0, p1 = dlp.Problem(3000, 4, 3, 11), dlp.Problem(2000, 7, 6, 3)
+    want0 = alone(p0)
+    eng = dlp.Engine(4, max_iterations=MAX_ITER)
+    g0, g1 = eng.add_problem(p0), eng.add_problem(p1)
+    for b in range(len(p0.batches)):
+        eng.step([(g0, b, p0.batches[b])])
+    L = N.lib()
+    size1 = int(L.dlp_engine_graph_resident_bytes(eng._h, g1))
+    req = max(24 * bt.edge_src.size + 2 * bt.nbytes() + 8 * bt.deleted.size + 4096 for bt in p1.batches)
+    srv = dlp.Server(eng, memory_budget_bytes=size1 + 4 * req, evict_idle=True)
+    rid = srv.submit(g1, 0, p1.batches[0])
+    srv.drain()
+    assert srv.result(rid)["status"] == 0
+    assert srv.evictions()[0] == 1 and eng.bytes_in_use <= size1 + 4 * req
+    g2 = eng.add_problem(dlp.Problem(1000, 3, 5, 7))
+    assert g2 not in (g0, g1)
+    srv.make_resident(g0)
+    assert eng.labels(g0).tobytes() == want0[-1][1].tobytes()
+    srv.close()

@@ -94,3 +94,33 @@ def test_autotune_picks_a_measured_candidate(gpu):
     assert all(c["ms"] > 0 for c in r["candidates"])
     best = min(r["candidates"], key=lambda c: c["ms"])
     assert (r["narrow_lanes"], r["blocks_per_sm"]) == (best["narrow_lanes"], best["blocks_per_sm"])
+
+
+@pytest.mark.gpu
+def test_multi_instance_sample_matches_oracle(gpu, oracle):
+    """16 graphs of the 512-graph multi-instance set (n log-uniform on
+    [1e3, 5e5], degree {3,5,7}, seeds i): the smallest, the largest and 14
+    evenly spaced by size between them, all stepped together in one launch per
+    step for all 10 batches, each checked against its own oracle run. A
+    second engine runs every pass on the full grid with 4-lane groups.
+    Propagation is capped at 1,000 passes per batch on both sides (the
+    workload's 100,000 would keep the oracle busy for many minutes on the
+    batches that never converge); everything else is the workload's."""
+    import bench
+    specs = bench.mix_sizes(512, 1e3, 5e5, 1000003)
+    order = sorted(range(len(specs)), key=lambda i: specs[i][0])
+    pick = [order[round(k * (len(order) - 1) / 15)] for k in range(16)]
+    probs = [dlp.Problem(*specs[i]) for i in pick]
+    cap = 1000
+    orcs = [oracle.OracleRun.from_problem(p, threads=0, max_iterations=cap) for p in probs]
+    engines = [dlp.Engine(len(probs), max_iterations=cap),
+               dlp.Engine(len(probs), max_iterations=cap, small_frontier_solo=0, narrow_lanes=4)]
+    gids = [[e.add_problem(p) for p in probs] for e in engines]
+    for b in range(10):
+        want = [(o.apply(b, p.batches[b]), o.labels()) for o, p in zip(orcs, probs)]
+        for e, ids in zip(engines, gids):
+            stats = e.step([(g, b, p.batches[b]) for g, p in zip(ids, probs)])
+            for i, (st, g) in enumerate(zip(stats, ids)):
+                for k in EXACT:
+                    assert st[k] == want[i][0][k], (specs[pick[i]], b, k, st[k], want[i][0][k])
+                assert e.labels(g).tobytes() == want[i][1].tobytes(), (specs[pick[i]], b)

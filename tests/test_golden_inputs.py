@@ -73,3 +73,18 @@ def test_oracle_host_rebuild_matches_reference(native, oracle, key):
         assert sha(run.artefact(oracle.ART_COL_IND)) == ga["col_ind"], b
         assert sha(run.artefact(oracle.ART_VALUES)) == ga["values"], b
         assert sha(run.artefact(oracle.ART_STATUS)) == ga["status"], b
+
+
+@pytest.mark.parametrize("key", sorted(DIGESTS["configs"]))
+def test_oracle_generator_matches_reference(oracle, key):
+    """The oracle's own restatement of the generator (used where the product
+    library must not be loaded) makes the reference's inputs too."""
+    g = DIGESTS["configs"][key]
+    p = oracle.OracleProblem(*g["args"])
+    assert p.num_nodes == g["n"] and p.num_edges == g["num_edges"]
+    for name in ("row_ptr", "col_ind", "values", "true_labels"):
+        assert sha(getattr(p, name)) == g[name], name
+    assert len(p.batches) == len(g["batches"])
+    for b, gb in zip(p.batches, g["batches"]):
+        for f in FIELDS:
+            assert sha(getattr(b, f)) == gb[f], (b, f)

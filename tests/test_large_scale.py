@@ -2,8 +2,10 @@
 vertices, average degree 7, the first batches of the 100-batch sequence
 (seed 42).
 
-The oracle cannot replay this size within a test, so correctness here rests
-on properties that hold at any size and fail on any race or indexing slip:
+The oracle replays only the first batches of this size within a test
+(test_largest_configuration_first_batches_match_oracle, below); beyond them
+correctness rests on properties that hold at any size and fail on any race or
+indexing slip:
 1. The arithmetic must not depend on the launch shape. A one-graph engine
    with 8-lane row groups and an engine with 4-lane groups must give
    bit-identical statistics and labels. The second engine also shares every
@@ -52,3 +54,25 @@ def test_largest_configuration_properties(gpu):
     for k in range(BATCHES):
         bt = p.batches[k]
         assert np.array_equal(la[bt.gt_ids], bt.gt_labels)
+
+
+ORACLE_BATCHES = 6
+
+
+@pytest.mark.gpu
+def test_largest_configuration_first_batches_match_oracle(gpu, oracle):
+    """The first batches of the 20,000,000-vertex problem against the oracle
+    (all host threads), element by element, in two launch shapes: the default
+    (small frontiers on one block or a 16-block sub-grid) and every pass on
+    the full grid with 4-lane row groups."""
+    from parity_checks import check_batch
+    p = dlp.Problem(20_000_000, 7, 100, 42)
+    orc = oracle.OracleRun.from_problem(p, record=True, threads=0)
+    runs = [dlp.Session.from_problem(p, record=True),
+            dlp.Session.from_problem(p, record=True, small_frontier_solo=0, narrow_lanes=4)]
+    for b in range(ORACLE_BATCHES):
+        want = orc.apply(b, p.batches[b])
+        for sess in runs:
+            got = sess.apply(b, p.batches[b])
+            check_batch(b, got, want, sess, orc, oracle)
+        assert want["affected_edges"] > 0 or b == 0

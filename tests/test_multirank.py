@@ -70,3 +70,29 @@ def test_two_gloo_ranks_reduce_shard_metrics():
         assert total == want_total
         assert slowest == 2.0
         assert count == 16.0
+
+
+def test_bench_gpus_flag_launches_that_many_ranks():
+    """`bench.py --gpus 2` (no WORLD_SIZE in the environment) starts two ranks
+    itself; the shard-check arm does no GPU work, so the launcher, the shard
+    split and the metric reductions run here on CPU with gloo."""
+    pytest.importorskip("torch")
+    import json
+    import subprocess
+    import bench
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "shard-check", "--gpus", "2"],
+                         capture_output=True, text=True, timeout=300, env=env)
+    assert out.returncode == 0, out.stderr
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1  # rank 0 alone prints
+    got = json.loads(lines[0])
+    specs = bench.mix_sizes(512, 1e3, 5e5, 1000003)
+    assert got["n_gpus"] == 2 and got["graphs"] == 512
+    assert got["total_load"] == sum(s[0] * s[1] for s in specs)
+    assert sorted(set(got["owners"])) == [1, 2]  # every graph owned by exactly one of the two ranks
+    for r in (0, 1):
+        mine = bench.shard_graphs(specs, r, 2)
+        assert all(got["owners"][i] == r + 1 for i in mine)
+    assert got["max_load"] == max(sum(specs[i][0] * specs[i][1] for i in bench.shard_graphs(specs, r, 2))
+                                  for r in (0, 1))
