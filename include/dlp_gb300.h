@@ -116,7 +116,14 @@ typedef struct dlp_config {
   int small_frontier_solo; /* bit 0: passes over small frontiers run on one
                               thread block with block barriers; bit 1: passes
                               over mid-size frontiers run on a sub-grid with its
-                              own barrier. Default 3 (both); same results. */
+                              own barrier; bit 2: within the one-block mode,
+                              frontiers of at most 64 loaded rows run on 8 warps
+                              with a named barrier. Default 7 (all); same
+                              results. */
+  int solo_entry;        /* one-block mode for total frontiers of at most this
+                            many vertices; 0 = 512, at most 1024 (autotuned) */
+  int subgrid_entry;     /* sub-grid mode for total frontiers of at most this
+                            many; 0 = 2048, at most 4096 (autotuned) */
 } dlp_config;
 
 void dlp_config_default(dlp_config *cfg);
@@ -266,20 +273,27 @@ int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, 
 
 /* Autotuner (no counterpart in the reference, whose launch shapes are fixed).
  * Propagation sends rows of at most 32 live entries to groups of
- * narrow_lanes lanes and longer rows to whole warps; the lane width of that
- * short-row bucket and the persistent grid's blocks per SM are chosen by
- * timing every candidate (lanes 4/8/16 x the blocks per SM the build allows) on a sample the
- * library generates with the reference generator: num_graphs graphs of
- * sizes[i] vertices and average degree degrees[i], `batches` batches each,
- * propagation capped at max_iterations passes per batch for the trial. Every
- * candidate must give identical statistics (checked). The fastest is written
- * into cfg->narrow_lanes and cfg->blocks_per_sm; other fields are kept. */
+ * narrow_lanes lanes and longer rows to whole warps, and runs each pass on one
+ * block, a 16-block sub-grid or the whole grid by the size of the frontier.
+ * The lane width of the short-row bucket, the two frontier thresholds
+ * (solo_entry, subgrid_entry) and the persistent grid's blocks per SM are
+ * chosen by timing every candidate (lanes 4/8/16 x one-block entry
+ * 256/512/1024 x sub-grid entry 1024/2048/4096 x the blocks per SM the build
+ * allows) on a sample the library generates with the reference generator:
+ * num_graphs graphs of sizes[i] vertices and average degree degrees[i],
+ * `batches` batches each, propagation capped at max_iterations passes per
+ * batch for the trial. Every candidate must give identical statistics
+ * (checked). The fastest is written into cfg->narrow_lanes,
+ * cfg->blocks_per_sm, cfg->solo_entry and cfg->subgrid_entry; other fields are
+ * kept. */
 typedef struct {
   int candidates;
   int best;               /* index of the chosen candidate */
-  int lanes[8];
-  int blocks_per_sm[8];
-  double ms[8];           /* summed device time of the sample's steps */
+  int lanes[32];
+  int blocks_per_sm[32];
+  int solo_entry[32];
+  int subgrid_entry[32];
+  double ms[32];          /* summed device time of the sample's steps */
 } dlp_tune_report;
 int dlp_autotune(dlp_config *cfg, int num_graphs, const int *sizes, const int *degrees, int batches,
                  int max_iterations, dlp_tune_report *report);

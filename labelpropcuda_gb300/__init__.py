@@ -117,7 +117,8 @@ class Session:
     def __init__(self, num_nodes: int, row_ptr, col_ind, values, true_labels=None, vertex_batch_map=None, *,
                  tau: float = -1.0, delta: float = 1e-4, max_iterations: int = 100000,
                  semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False, narrow_lanes: int = 0,
-                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: int = 3):
+                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: int = 7,
+                 solo_entry: int = 0, subgrid_entry: int = 0):
         L = _n.lib()
         cfg = _n.Config()
         L.dlp_config_default(ctypes.byref(cfg))
@@ -125,6 +126,7 @@ class Session:
         cfg.semantics, cfg.device, cfg.record = semantics, device, int(bool(record))
         cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
         cfg.small_frontier_solo = int(small_frontier_solo)
+        cfg.solo_entry, cfg.subgrid_entry = int(solo_entry), int(subgrid_entry)
         self._keep = [np.ascontiguousarray(row_ptr, dtype=np.int32), np.ascontiguousarray(col_ind, dtype=np.int32),
                       np.ascontiguousarray(values, dtype=np.float32)]
         tl = None if true_labels is None else np.ascontiguousarray(true_labels, dtype=np.float32)
@@ -217,7 +219,7 @@ class Engine:
     def __init__(self, max_graphs: int, memory_budget_bytes: int = 0, *, tau: float = -1.0, delta: float = 1e-4,
                  max_iterations: int = 100000, semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False,
                  narrow_lanes: int = 0, blocks_per_sm: int = 0, wait_timeout_s: float = 2.0,
-                 small_frontier_solo: int = 3):
+                 small_frontier_solo: int = 7, solo_entry: int = 0, subgrid_entry: int = 0):
         L = _n.lib()
         cfg = _n.Config()
         L.dlp_config_default(ctypes.byref(cfg))
@@ -225,6 +227,7 @@ class Engine:
         cfg.semantics, cfg.device, cfg.record = semantics, device, int(bool(record))
         cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
         cfg.small_frontier_solo = int(small_frontier_solo)
+        cfg.solo_entry, cfg.subgrid_entry = int(solo_entry), int(subgrid_entry)
         self._h = ctypes.c_void_p()
         _n.check(L.dlp_engine_create(ctypes.byref(cfg), max_graphs, memory_budget_bytes, ctypes.byref(self._h)))
         self.sizes: dict[int, int] = {}
@@ -361,9 +364,12 @@ class Engine:
 
 def autotune(sizes: list[int], degrees: list[int], batches: int = 10, max_iterations: int = 2000,
              **config) -> dict:
-    """Times every launch-shape candidate (lanes per short row x blocks per
-    SM) on a generated sample of the given graph sizes and degrees and
-    returns the fastest as {"narrow_lanes", "blocks_per_sm", "candidates"}."""
+    """Times every launch-shape candidate (lanes per short row x one-block
+    and sub-grid frontier thresholds x blocks per SM) on a generated sample of
+    the given graph sizes and degrees and returns the fastest as
+    {"narrow_lanes", "blocks_per_sm", "engine_kw": {solo_entry, subgrid_entry},
+    "candidates"}; every candidate gave the same statistics (checked by the
+    library)."""
     L = _n.lib()
     cfg = _n.Config()
     L.dlp_config_default(ctypes.byref(cfg))
@@ -374,9 +380,10 @@ def autotune(sizes: list[int], degrees: list[int], batches: int = 10, max_iterat
     dg = (ctypes.c_int * n)(*degrees)
     rep = _n.TuneReport()
     _n.check(L.dlp_autotune(ctypes.byref(cfg), n, sz, dg, batches, max_iterations, ctypes.byref(rep)))
-    cands = [{"narrow_lanes": rep.lanes[i], "blocks_per_sm": rep.blocks_per_sm[i], "ms": rep.ms[i]}
-             for i in range(rep.candidates)]
-    return {"narrow_lanes": cfg.narrow_lanes, "blocks_per_sm": cfg.blocks_per_sm, "candidates": cands}
+    cands = [{"narrow_lanes": rep.lanes[i], "blocks_per_sm": rep.blocks_per_sm[i], "solo_entry": rep.solo_entry[i],
+              "subgrid_entry": rep.subgrid_entry[i], "ms": rep.ms[i]} for i in range(rep.candidates)]
+    return {"narrow_lanes": cfg.narrow_lanes, "blocks_per_sm": cfg.blocks_per_sm,
+            "engine_kw": {"solo_entry": cfg.solo_entry, "subgrid_entry": cfg.subgrid_entry}, "candidates": cands}
 
 
 def device_name(device: int = 0) -> str:

@@ -34,6 +34,7 @@ class Config(ctypes.Structure):
         ("semantics", ctypes.c_int), ("device", ctypes.c_int), ("record", ctypes.c_int),
         ("narrow_lanes", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
         ("wait_timeout_s", ctypes.c_double), ("small_frontier_solo", ctypes.c_int),
+        ("solo_entry", ctypes.c_int), ("subgrid_entry", ctypes.c_int),
     ]
 
 
@@ -77,8 +78,9 @@ class RequestResult(ctypes.Structure):
 
 class TuneReport(ctypes.Structure):
     _fields_ = [
-        ("candidates", ctypes.c_int), ("best", ctypes.c_int), ("lanes", ctypes.c_int * 8),
-        ("blocks_per_sm", ctypes.c_int * 8), ("ms", ctypes.c_double * 8),
+        ("candidates", ctypes.c_int), ("best", ctypes.c_int), ("lanes", ctypes.c_int * 32),
+        ("blocks_per_sm", ctypes.c_int * 32), ("solo_entry", ctypes.c_int * 32),
+        ("subgrid_entry", ctypes.c_int * 32), ("ms", ctypes.c_double * 32),
     ]
 
 

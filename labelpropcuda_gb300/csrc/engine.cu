@@ -387,7 +387,9 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
   args.ng_new = count;
   args.ectl = e->ectl;
   args.timeout_ns = static_cast<unsigned long long>(to * 1e9);
-  args.solo = e->cfg.small_frontier_solo < 0 ? 3 : e->cfg.small_frontier_solo;
+  args.solo = e->cfg.small_frontier_solo < 0 ? 7 : e->cfg.small_frontier_solo;
+  args.solo_entry = e->cfg.solo_entry > 0 ? e->cfg.solo_entry : dlp::engine::kSoloEntryDefault;
+  args.sub_entry = e->cfg.subgrid_entry > 0 ? e->cfg.subgrid_entry : dlp::engine::kSubEntryDefault;
   args.pass_budget = opts.pass_budget;
   args.slice_ns = opts.slice_ns;
   args.tag = e->steps + 1;
@@ -562,7 +564,7 @@ void dlp_config_default(dlp_config *cfg) {
   cfg->max_iterations = 100000;
   cfg->semantics = DLP_SEMANTICS_REF;
   cfg->wait_timeout_s = 2.0;
-  cfg->small_frontier_solo = 3;
+  cfg->small_frontier_solo = 7;
 }
 
 int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_budget_bytes, dlp_engine **out) {
@@ -578,6 +580,9 @@ int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_bu
   const int lanes = cfg.narrow_lanes == 0 ? 8 : cfg.narrow_lanes;
   if (lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "narrow_lanes must be 4, 8, 16 or 32");
+  if (cfg.solo_entry < 0 || cfg.solo_entry > dlp::engine::kSoloEntryMax || cfg.subgrid_entry < 0 ||
+      cfg.subgrid_entry > dlp::engine::kSubEntryMax)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "solo_entry must be in [0, 1024] and subgrid_entry in [0, 4096]");
   DLP_CUDA_TRY(cudaSetDevice(cfg.device));
   DLP_TRY(dlp::require_device());
   dlp_engine *e = new dlp_engine();

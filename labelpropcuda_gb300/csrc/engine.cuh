@@ -26,6 +26,14 @@ namespace dlp {
 namespace engine {
 
 constexpr int kMaxGraphs = 1024;
+// Frontier sizes below which propagation passes leave the full grid: the
+// one-block mode (default 512, at most kSoloEntryMax) and the 16-block
+// sub-grid mode (default 2048, at most kSubEntryMax). Tunable per engine.
+constexpr int kSoloEntryDefault = 512;
+constexpr int kSoloEntryMax = 1024;
+constexpr int kSubEntryDefault = 2048;
+constexpr int kSubEntryMax = 4096;
+constexpr int kSubLive = 4096;  // the sub-grid mode leaves once the frontier grows above this
 
 struct GraphRec {
   session::DevState st;
@@ -59,7 +67,9 @@ struct EngineArgs {
   int ng_new;   // the first ng_new of them start a batch; the rest continue one
   EngineCtl *ectl;
   unsigned long long timeout_ns;
-  int solo;  // bit 0: one-block passes for small frontiers; bit 1: sub-grid passes
+  int solo;  // bit 0: one-block passes for small frontiers; bit 1: sub-grid passes; bit 2: team passes
+  int solo_entry;  // total frontier at most this: one-block passes (<= kSoloEntryMax)
+  int sub_entry;   // total frontier at most this: sub-grid passes (<= kSubLive)
   int pass_budget;                // propagation passes this launch runs at most (0: no limit)
   unsigned long long slice_ns;    // propagation time after which the launch stops (0: no limit)
   int tag;                        // unique per launch (stop requests)

@@ -929,7 +929,8 @@ constexpr int kRP = 4096;          // row-pool entries
 // need more entries than the table has slots in use
 constexpr int kSoloList = kVTUse;
 static_assert(kSoloList >= kVTUse, "a one-block frontier list must hold every slot in use");
-constexpr int kSoloEntry = 512;    // enter when the total frontier is at most this
+static_assert(kSoloEntryMax <= kVTUse && kSoloEntryMax <= kSoloList,
+              "a one-block stint starts by putting the whole frontier into the vertex table and list 0");
 constexpr int kSoloMaxPasses = 65000;  // per stint, so that per-slot visit counts fit 16 bits
 constexpr unsigned long long kSoloBudgetNs = 100000000ull;
 constexpr unsigned long long kEmptyKey = ~0ull;
@@ -963,6 +964,7 @@ struct SoloCache {
   int rp_top;                    // row-pool entries in use
   int stop_at;                   // stint pass at which a time budget stops the stint
   int stop_slice;                // that budget was the launch's time slice
+  int team_end;                  // first pass a team stint did not run
 };
 
 __device__ __forceinline__ unsigned mix64(unsigned long long x) {
@@ -1001,19 +1003,19 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
 }
 
 // One pass of the one-block mode over the rows of `cur` (cnt entries), G lanes
-// per row: every row from shared memory, marks into `next` and the counters of
-// list nq. G only sets how the rows are spread over the block's threads; the
-// arithmetic and the marked set do not depend on it.
-template <int G>
+// per row, by the block's first NW warps: every row from shared memory, marks
+// into `next` and the counters of list nq. G and NW only set how the rows are
+// spread over the threads; the arithmetic and the marked set do not depend on
+// them.
+template <int G, int NW>
 __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, const unsigned short *cur,
                                           unsigned short *next, int cnt, int nq, int k, bool rec_any) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int kWarps = kBlock / 32;
   constexpr int R = 32 / G;
   constexpr int GPW = 32 / G;
   const int grp = lane / G, gl = lane & (G - 1);
 
-  for (int base = warp * GPW; base < cnt; base += kWarps * GPW) {
+  for (int base = warp * GPW; base < cnt; base += NW * GPW) {
     const int item = base + grp;
     const bool valid = item < cnt;
     const int su = valid ? cur[item] : 0;
@@ -1081,7 +1083,6 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
         if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
       }
     }
-    const int nf = __popc(fresh);
     int add = 0, wide = 0;
 #pragma unroll
     for (int r = 0; r < R + 1; ++r)
@@ -1091,33 +1092,117 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
         if (l == kWideLen) wide = 1;
         else if (c.row[ns] == kNoRow) add += l;
       }
-    int incl = nf;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += t;
-    }
-    const int tot = __shfl_sync(0xffffffffu, incl, 31);
     add = __reduce_add_sync(0xffffffffu, add);
     wide = __reduce_or_sync(0xffffffffu, wide);
-    int at = 0;
-    if (lane == 31 && tot) {
-      at = atomicAdd(&c.cnt[nq], tot);
-      if (add) atomicAdd(&c.need[nq], add);
-      if (wide) c.wide[nq] = 1;
-    }
-    at = __shfl_sync(0xffffffffu, at, 31) + incl - nf;
+    if constexpr (R <= 8) {
+      // one ballot per candidate slot (independent, unlike a shuffle scan):
+      // the warp's fresh marks of slot r take a run of the reservation, in
+      // lane order
+      unsigned bal[R + 1];
+      int tot = 0;
 #pragma unroll
-    for (int r = 0; r < R + 1; ++r)
-      if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
+      for (int r = 0; r < R + 1; ++r) {
+        bal[r] = __ballot_sync(0xffffffffu, (fresh >> r) & 1u);
+        tot += __popc(bal[r]);
+      }
+      int at = 0;
+      if (lane == 0 && tot) {
+        at = atomicAdd(&c.cnt[nq], tot);
+        if (add) atomicAdd(&c.need[nq], add);
+        if (wide) c.wide[nq] = 1;
+      }
+      at = __shfl_sync(0xffffffffu, at, 0);
+      const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r) {
+        if ((fresh >> r) & 1u) next[at + __popc(bal[r] & below)] = static_cast<unsigned short>(r < R ? vv[r] : su);
+        at += __popc(bal[r]);
+      }
+    } else {
+      // many slots per lane: a scan of the per-lane counts keeps fewer values live
+      const int nf = __popc(fresh);
+      int incl = nf;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int tot = __shfl_sync(0xffffffffu, incl, 31);
+      int at = 0;
+      if (lane == 31 && tot) {
+        at = atomicAdd(&c.cnt[nq], tot);
+        if (add) atomicAdd(&c.need[nq], add);
+        if (wide) c.wide[nq] = 1;
+      }
+      at = __shfl_sync(0xffffffffu, at, 31) + incl - nf;
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r)
+        if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
+    }
   }
+}
+
+// Team mode of the one-block passes: a small frontier whose rows are all in
+// the row pool is run by the block's first kTeamWarps warps, with a named
+// barrier (id 1) of those warps between passes, while the other warps of the
+// block wait at the block barrier that ends the team stint. The passes and
+// their arithmetic are those of the whole block; only fewer warps share the
+// rows, and the waiting warps take no issue slots from them.
+constexpr int kTeamWarps = 8;
+constexpr int kTeamRows = kTeamWarps * 32 / 4;  // rows one round of 4-lane groups takes
+
+__device__ __forceinline__ void team_barrier() {
+  asm volatile("bar.sync 1, %0;" ::"r"(kTeamWarps * 32) : "memory");
+}
+
+// Runs team passes from pass k (stint pass j = k - k0) while the frontier
+// stays small and loaded; returns the first pass not run. Called by the
+// threads of the first kTeamWarps warps only; every exit decision reads values
+// written before the last team barrier, so all of them leave together.
+__device__ int team_passes(const EngineArgs &e, SoloCache &c, int k0, int k, int max_iter, bool rec_any,
+                           uint64_t t0) {
+  const int tid = threadIdx.x;
+  const int ng = e.ng;
+  for (;; ++k) {
+    const int j = k - k0;
+    const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
+    const int cnt = c.cnt[q];
+    const int need = c.need[q];
+    if (cnt == 0 || cnt > kTeamRows || need > 0 || c.wide[q] || k >= max_iter || j >= kSoloMaxPasses ||
+        j >= c.stop_at || (e.pass_budget > 0 && k >= e.pass_budget) || c.used > kVTUse || c.rp_top > kRP)
+      break;
+    if (tid == 0) {
+      const int z = (j + 2) % 3;
+      c.cnt[z] = 0;
+      c.need[z] = 0;
+      c.wide[z] = 0;
+    }
+    if (rec_any)
+      for (int g = tid; g < ng; g += kTeamWarps * 32) {
+        const GraphRec &r = e.recs[g];
+        const int kg = k + 1 + r.ba.pass0;
+        if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
+      }
+    const unsigned short *cur = c.list[p];
+    unsigned short *next = c.list[p ^ 1];
+    if (cnt <= kTeamWarps * 4) solo_rows<8, kTeamWarps>(e, c, cur, next, cnt, nq, k, rec_any);
+    else solo_rows<4, kTeamWarps>(e, c, cur, next, cnt, nq, k, rec_any);
+    if (tid == 0 && (j & 15) == 15) {
+      if (global_timer_ns() - t0 > kSoloBudgetNs) c.stop_at = j + 1;
+      if (slice_over(e)) {
+        c.stop_at = j + 1;
+        c.stop_slice = 1;
+      }
+    }
+    team_barrier();
+  }
+  return k;
 }
 template <int G>
 __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c) {
   const int ng = e.ng;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int kWarps = kBlock / 32;
-  constexpr int R = 32 / G;
   constexpr int GPW = 32 / G;
   const int grp = lane / G, gl = lane & (G - 1);
   for (int i = tid; i < kVT; i += kBlock) c.key[i] = kEmptyKey;
@@ -1173,6 +1258,7 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   __syncthreads();
   const uint64_t t0 = global_timer_ns();
   int k = k0;
+  int team_from = (e.solo & 4) ? k0 : 0x7fffffff;  // team mode is not tried before this pass
   for (;; ++k) {
     const int j = k - k0;
     const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
@@ -1183,6 +1269,17 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     if (cnt == 0 || cnt > kSoloList || k >= max_iter || c.wide[q] || j >= kSoloMaxPasses || j >= c.stop_at ||
         (e.pass_budget > 0 && k >= e.pass_budget) || c.used + need > kVTUse || c.rp_top + need > kRP)
       break;
+    if (need == 0 && cnt <= kTeamRows && k >= team_from) {
+      if (warp < kTeamWarps) {
+        const int kk = team_passes(e, c, k0, k, max_iter, rec_any, t0);
+        if (tid == 0) c.team_end = kk;
+      }
+      __syncthreads();  // the other warps wait here for the whole team stint
+      const int kk = c.team_end;
+      if (kk == k) team_from = k + 1;  // no pass taken: the block runs this one
+      k = kk - 1;  // the loop increment resumes at pass kk
+      continue;
+    }
     if (need > 0) {
       __syncthreads();  // every thread has read used / rp_top above
       // load the rows of frontier vertices seen for the first time
@@ -1230,9 +1327,9 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     // (8 lanes up to 64 rows, 4 up to 128, else 2)
     const unsigned short *cur = c.list[p];
     unsigned short *next = c.list[p ^ 1];
-    if (cnt <= kBlock / 8) solo_rows<8>(e, c, cur, next, cnt, nq, k, rec_any);
-    else if (cnt <= kBlock / 4) solo_rows<4>(e, c, cur, next, cnt, nq, k, rec_any);
-    else solo_rows<2>(e, c, cur, next, cnt, nq, k, rec_any);
+    if (cnt <= kBlock / 8) solo_rows<8, kWarps>(e, c, cur, next, cnt, nq, k, rec_any);
+    else if (cnt <= kBlock / 4) solo_rows<4, kWarps>(e, c, cur, next, cnt, nq, k, rec_any);
+    else solo_rows<2, kWarps>(e, c, cur, next, cnt, nq, k, rec_any);
     // time budgets: checked by thread 0, they stop the stint two passes on
     // (a thread still at the top of this pass must not see the request)
     if (tid == 0 && (j & 15) == 15) {
@@ -1390,8 +1487,7 @@ __device__ __forceinline__ void pass_sizes(const EngineArgs &e, int k, int *pref
 // with their own (cheaper) barrier while the other blocks wait at the next
 // grid barrier; the passes are those of the full grid.
 constexpr int kSubBlocks = 16;
-constexpr int kSubEntry = 2048;   // enter when the total frontier is at most this
-constexpr int kSubLive = 4096;    // leave when it grows above this
+static_assert(kSubEntryMax <= kSubLive, "the sub-grid mode leaves above kSubLive");
 
 template <int G>
 __device__ bool sub_passes(const EngineArgs &e, int k0, int slot, int solo_from, int *pref, int *pref2) {
@@ -1407,7 +1503,7 @@ __device__ bool sub_passes(const EngineArgs &e, int k0, int slot, int solo_from,
     if (tn + tw == 0 || tn + tw > kSubLive || stop || (e.pass_budget > 0 && k >= e.pass_budget)) break;
     // a frontier the one-block mode can take goes back to it (cheaper passes),
     // unless that mode recently could not hold its working set
-    if (k > k0 && (e.solo & 1) && tn + tw <= kSoloEntry && k >= solo_from) break;
+    if (k > k0 && (e.solo & 1) && tn + tw <= e.solo_entry && k >= solo_from) break;
     run_pass<G>(e, k, pref, tn, pref2, tw, lane, warp0 + (threadIdx.x >> 5), nwarps, t0, nthreads);
     if (t0 == 0 && ((k - k0) & 31) == 31 && global_timer_ns() - start > 100000000ull)
       e.ectl->sub_stop = stop_code(e, k + 1);
@@ -1439,8 +1535,8 @@ __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2
     if (e.pass_budget > 0 && k >= e.pass_budget) break;
     if (ld_relaxed_u64(&e.ectl->slice_stop) == stop_code(e, k)) break;
     if (c.gtid == 0) e.ectl->where_pass = k;
-    const bool solo_ok = (e.solo & 1) && tn + tw <= kSoloEntry && k != no_small_at && k >= solo_from;
-    const bool sub_ok = !solo_ok && (e.solo & 2) && gridDim.x > 2 * kSubBlocks && tn + tw <= kSubEntry &&
+    const bool solo_ok = (e.solo & 1) && tn + tw <= e.solo_entry && k != no_small_at && k >= solo_from;
+    const bool sub_ok = !solo_ok && (e.solo & 2) && gridDim.x > 2 * kSubBlocks && tn + tw <= e.sub_entry &&
                         k != no_small_at;
     if (solo_ok || sub_ok) {
       if (solo_ok) {

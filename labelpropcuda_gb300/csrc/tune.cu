@@ -4,8 +4,11 @@
 //
 // The engine's propagation splits rows into two degree buckets: rows of at
 // most 32 live entries go to groups of `narrow_lanes` lanes (4, 8, 16 or 32),
-// longer rows to whole warps. The lane width of the short-row bucket and the
-// persistent grid's blocks per SM are the tunables: the best choice depends on
+// longer rows to whole warps. Each pass also picks its launch mode by the
+// total frontier: one block (up to solo_entry vertices), a 16-block sub-grid
+// (up to subgrid_entry) or the whole grid. The tunables are the lane width of
+// the short-row bucket, the two frontier thresholds and the persistent grid's
+// blocks per SM (one for the 1,024-thread build): the best choice depends on
 // the row lengths and frontier sizes of the workload. The tuner builds a
 // sample workload with the reference generator (graph sizes and degrees given
 // by the caller), times every candidate on it with CUDA events (the engine's
@@ -19,6 +22,8 @@
 #include "session_kernel.cuh"
 
 namespace {
+
+constexpr int kTuneMaxCandidates = 32;  // the report's capacity
 
 struct ProblemDeleter {
   void operator()(dlp_problem *p) const { dlp_problem_free(p); }
@@ -109,6 +114,8 @@ int dlp_autotune(dlp_config *cfg, int num_graphs, const int *sizes, const int *d
     bmaps.push_back(std::move(m));
   }
   static const int kLanes[] = {4, 8, 16};
+  static const int kSoloEntries[] = {256, 512, 1024};
+  static const int kSubEntries[] = {1024, 2048, 4096};
   // blocks per SM the build's block size allows (1024-thread blocks: one)
   std::vector<int> kBlocks = {1};
   if (dlp::session::kBlock <= 512) kBlocks.insert(kBlocks.begin(), 2);
@@ -117,29 +124,38 @@ int dlp_autotune(dlp_config *cfg, int num_graphs, const int *sizes, const int *d
   std::vector<dlp_batch_stats> ref_stats;
   double best = -1.0;
   for (int bl : kBlocks)
-    for (int ln : kLanes) {
-      dlp_config c = *cfg;
-      c.narrow_lanes = ln;
-      c.blocks_per_sm = bl;
-      c.max_iterations = max_iterations;
-      c.record = 0;
-      double ms = 0.0;
-      std::vector<dlp_batch_stats> st;
-      DLP_TRY(trial(c, probs, batches, bmaps, &ms, &st));
-      if (ref_stats.empty()) ref_stats = st;
-      else if (!same_stats(ref_stats, st))
-        return dlp::fail(DLP_ERR_INTERNAL, "launch shapes disagree on the sample's statistics");
-      const int k = rep.candidates++;
-      rep.lanes[k] = ln;
-      rep.blocks_per_sm[k] = bl;
-      rep.ms[k] = ms;
-      if (best < 0.0 || ms < best) {
-        best = ms;
-        rep.best = k;
-      }
-    }
+    for (int ln : kLanes)
+      for (int se : kSoloEntries)
+        for (int ge : kSubEntries) {
+          if (rep.candidates >= kTuneMaxCandidates) break;
+          dlp_config c = *cfg;
+          c.narrow_lanes = ln;
+          c.blocks_per_sm = bl;
+          c.solo_entry = se;
+          c.subgrid_entry = ge;
+          c.max_iterations = max_iterations;
+          c.record = 0;
+          double ms = 0.0;
+          std::vector<dlp_batch_stats> st;
+          DLP_TRY(trial(c, probs, batches, bmaps, &ms, &st));
+          if (ref_stats.empty()) ref_stats = st;
+          else if (!same_stats(ref_stats, st))
+            return dlp::fail(DLP_ERR_INTERNAL, "launch shapes disagree on the sample's statistics");
+          const int k = rep.candidates++;
+          rep.lanes[k] = ln;
+          rep.blocks_per_sm[k] = bl;
+          rep.solo_entry[k] = se;
+          rep.subgrid_entry[k] = ge;
+          rep.ms[k] = ms;
+          if (best < 0.0 || ms < best) {
+            best = ms;
+            rep.best = k;
+          }
+        }
   cfg->narrow_lanes = rep.lanes[rep.best];
   cfg->blocks_per_sm = rep.blocks_per_sm[rep.best];
+  cfg->solo_entry = rep.solo_entry[rep.best];
+  cfg->subgrid_entry = rep.subgrid_entry[rep.best];
   if (report) *report = rep;
   return DLP_OK;
 }

@@ -85,15 +85,20 @@ def test_budget_admission_and_removal(gpu):
 
 @pytest.mark.gpu
 def test_autotune_picks_a_measured_candidate(gpu):
-    """The tuner times every launch shape on a generated sample; all of them
-    must agree on the statistics (checked inside) and the choice is the
-    fastest measured one."""
+    """The tuner times every launch shape (lane width x one-block and sub-grid
+    thresholds) on a generated sample; all of them must agree on the
+    statistics (checked inside) and the choice is the fastest measured one."""
     r = dlp.autotune([3000, 1000, 2000], [5, 3, 7], batches=5, max_iterations=300)
-    shapes = {(c["narrow_lanes"], c["blocks_per_sm"]) for c in r["candidates"]}
-    assert len(shapes) == len(r["candidates"]) >= 3  # every candidate a distinct launch shape
+    key = lambda c: (c["narrow_lanes"], c["blocks_per_sm"], c["solo_entry"], c["subgrid_entry"])
+    shapes = {key(c) for c in r["candidates"]}
+    assert len(shapes) == len(r["candidates"]) >= 27  # every candidate a distinct launch shape
     assert all(c["ms"] > 0 for c in r["candidates"])
     best = min(r["candidates"], key=lambda c: c["ms"])
-    assert (r["narrow_lanes"], r["blocks_per_sm"]) == (best["narrow_lanes"], best["blocks_per_sm"])
+    chosen = (r["narrow_lanes"], r["blocks_per_sm"], r["engine_kw"]["solo_entry"], r["engine_kw"]["subgrid_entry"])
+    assert chosen == key(best)
+    # the chosen shape is usable as engine settings
+    eng = dlp.Engine(2, narrow_lanes=r["narrow_lanes"], **r["engine_kw"])
+    eng.close()
 
 
 @pytest.mark.gpu

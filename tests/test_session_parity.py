@@ -62,18 +62,31 @@ def test_session_matches_oracle(gpu, oracle, cfg):
         assert gl.tobytes() == wl.tobytes(), (b, int(np.sum(gl != wl)), float(np.max(np.abs(gl - wl))))
 
 
+MODES = [
+    dict(),                                            # default: team, one-block, sub-grid, full grid
+    dict(small_frontier_solo=3),                       # one-block passes without the 8-warp team
+    dict(small_frontier_solo=1),                       # one-block only
+    dict(small_frontier_solo=0),                       # every pass on the full grid
+    dict(solo_entry=1024, subgrid_entry=4096),         # the largest thresholds
+    dict(solo_entry=256, subgrid_entry=1024, narrow_lanes=16),
+]
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("sem", [dlp.SEMANTICS_REF, dlp.SEMANTICS_SPEC])
-def test_solo_mode_gives_identical_results(gpu, sem):
-    """Small frontiers on one block (default) vs every pass on the whole grid."""
-    p = dlp.Problem(5000, 5, 10, 42)
-    a = dlp.Session.from_problem(p, semantics=sem, small_frontier_solo=True)
-    b = dlp.Session.from_problem(p, semantics=sem, small_frontier_solo=False)
+@pytest.mark.parametrize("n", [5000, 50000])
+def test_pass_modes_give_identical_results(gpu, sem, n):
+    """The passes give the same results whichever mode runs them: the 8-warp
+    team, the one-block mode, the sub-grid, the full grid, at any thresholds."""
+    p = dlp.Problem(n, 5, 10, 42)
+    runs = [dlp.Session.from_problem(p, semantics=sem, **m) for m in MODES]
     for i, bt in enumerate(p.batches):
-        sa, sb = a.apply(i, bt), b.apply(i, bt)
-        for k in EXACT_STATS:
-            assert sa[k] == sb[k], (i, k)
-        assert a.labels().tobytes() == b.labels().tobytes(), i
+        st = [r.apply(i, bt) for r in runs]
+        labs = [r.labels().tobytes() for r in runs]
+        for j in range(1, len(runs)):
+            for k in EXACT_STATS:
+                assert st[j][k] == st[0][k], (MODES[j], i, k)
+            assert labs[j] == labs[0], (MODES[j], i)
 
 
 @pytest.mark.gpu
