@@ -21,16 +21,22 @@ CPU counterpart is the oracle's restatement of it (oracle/, a port), run with
 all host threads on the same workload.
 
 Served vs plain (the `served` object of the same line; --no-served skips it):
-a mixed-graph stream of --served-graphs resident graphs (default 64; the
-multi-instance shape with 512 is --served-graphs 512), sizes log-uniform on
-[1e3, 5e5], degree {3,5,7}, 10 batches each. `batched` runs one engine launch
-per batch index over all graphs; `served_saturated` replays every request
-through the continuous-batching server with all of them queued at t = 0;
-`served_poisson` replays them with Poisson arrivals at half the saturated
+the multi-instance configuration, 512 resident graphs (n log-uniform on
+[1e3, 5e5], degree {3,5,7}, generator seed i, 10 batches each: 5,120
+requests). `batched` runs one engine launch per batch index over all graphs;
+`served_saturated` replays every request through the continuous-batching
+server with all of them queued at t = 0; `served_poisson_sweep` replays a
+size-stratified subset with Poisson arrivals at fractions of its saturated
 request rate (latency = finish - arrival); `plain` is the server in serial
 mode (one request at a time, run to its end — the plain per-batch path) on a
-bounded sample of whole graphs. All three count the same affected edges per
-request; the served paths include the host-to-device copy of every request.
+stratified sample of whole graphs, scaled to the whole trace. All count the
+same affected edges per request; the served paths include the host-to-device
+copy of every request. --gpus N (without WORLD_SIZE set) starts N ranks; the
+graphs are then split across them with no collective on the data path.
+
+Also on the line: the FP64 oracle's error on the headline workload, and the
+reference's own CUDA build (oracle/_ref/ref_kernels, built from a guarded copy
+of its sources when that copy is present) timed on the same GPU.
 """
 from __future__ import annotations
 
@@ -539,9 +545,9 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
       served_saturated the continuous-batching server with every request
                        queued at t = 0 (host-to-device copies included)
       served_poisson   the same server with Poisson arrivals at fractions of
-                       the saturated request rate, each over a fixed window of
-                       arrivals (a prefix of the request list, so every graph's
-                       batches keep their order); latency = finish - arrival
+                       the saturated request rate, over a size-stratified
+                       subset of the graphs (every k-th by vertex count, all
+                       its requests); latency = finish - arrival
       plain            the server in serial mode (one request at a time, run
                        to its end: the plain per-batch path) replaying the same
                        requests graph by graph, on a stratified sample of whole
@@ -637,15 +643,28 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
                   "service_ms_p99": dist_max(td, percentile(svc, 0.99))}
     progress(f"served saturated {served_sat['value'] / 1e9:.3f} G/s, makespan {span:.1f} s")
 
-    # Poisson sweep: offered rate = fraction x the saturated request rate,
-    # arrivals over a fixed window (a prefix of the batch-major request list)
-    sweep = []
+    # Poisson sweep over a size-stratified subset (every --sweep-stride-th
+    # graph by vertex count, all its batches): its own saturated run first,
+    # then Poisson arrivals at fractions of that request rate, every request
+    # of the subset in each run (batch-major order: every graph's batches keep
+    # their order)
+    by_size = sorted(range(len(gids)), key=lambda i: (probs[i].num_nodes, i))
+    sub = sorted(by_size[::max(1, args.sweep_stride)])
+    sub_reqs = [(0.0, gids[i], skip + b, probs[i].batches[b]) for b in range(nb) for i in sub]
+    res, sub_span = replay(sub_reqs)
+    sub_rate = len(res) / sub_span
+    sweep = [{"fraction_of_saturated": "saturated (all queued at t = 0)", "requests": int(dist_sum(td, len(res))),
+              "value": dist_sum(td, sum(r["stats"]["affected_edges"] for r in res)) / dist_max(td, sub_span),
+              "makespan_s": dist_max(td, sub_span),
+              "latency_ms_p50": dist_max(td, percentile([1e3 * (r["finish_s"] - r["arrival_s"]) for r in res], 0.5)),
+              "latency_ms_p99": dist_max(td, percentile([1e3 * (r["finish_s"] - r["arrival_s"]) for r in res],
+                                                        0.99))}]
+    progress(f"sweep subset: {len(sub)} graphs, {len(res)} requests, saturated {sub_rate:.1f} req/s")
     for frac in args.poisson_fractions:
-        rate = frac * sat_rate
+        rate = frac * sub_rate
         rng = np.random.default_rng(7)
-        times = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
-        keep = max(1, int(np.searchsorted(times, args.poisson_window_s, side="right")))
-        trace = [(float(t), g, b, bt) for t, (_, g, b, bt) in zip(times[:keep], reqs[:keep])]
+        times = np.cumsum(rng.exponential(1.0 / rate, len(sub_reqs)))
+        trace = [(float(t), g, b, bt) for t, (_, g, b, bt) in zip(times, sub_reqs)]
         res, span = replay(trace)
         lat = [1e3 * (r["finish_s"] - r["arrival_s"]) for r in res]
         p_ae = dist_sum(td, sum(r["stats"]["affected_edges"] for r in res))
@@ -700,7 +719,11 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
            "config": "multi-instance batching (512 graphs)" if args.served_shape == "mixed" and count == 512
            else f"{count} graphs",
            "setup_s": setup_s, "batched": batched, "served_saturated": served_sat,
-           "served_poisson_sweep": sweep, "poisson_window_s": args.poisson_window_s, "plain": plain,
+           "served_poisson_sweep": sweep,
+           "sweep_subset": f"{len(sub)} of {len(gids)} graphs (every {args.sweep_stride}th by vertex count), "
+                           f"{len(sub_reqs)} requests per run; Poisson arrivals (numpy seed 7) at fractions of the "
+                           f"subset's saturated request rate; latency = finish - arrival",
+           "plain": plain,
            "served_over_plain": served_sat["value"] / plain_v if plain_v else None,
            "batched_over_plain": batched["value"] / plain_v if plain_v else None,
            "p99_latency_ms_at_saturated_offer": sat_sweep[0]["latency_ms_p99"] if sat_sweep else None,
@@ -777,7 +800,7 @@ def main(argv=None) -> int:
     ap.add_argument("--slice-us", type=float, default=2000.0)
     ap.add_argument("--poisson-fractions", type=lambda x: [float(v) for v in x.split(",")],
                     default=[0.25, 0.5, 0.75, 1.0], help="offered rates as fractions of the saturated rate")
-    ap.add_argument("--poisson-window-s", type=float, default=15.0, help="arrival window of each Poisson run")
+    ap.add_argument("--sweep-stride", type=int, default=4, help="Poisson sweep over every k-th graph by size")
     ap.add_argument("--plain-per-stratum", type=int, default=3)
     ap.add_argument("--plain-strata", type=int, default=8)
     ap.add_argument("--no-reference-cuda", action="store_true",

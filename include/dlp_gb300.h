@@ -333,8 +333,10 @@ typedef struct dlp_server dlp_server;
 typedef struct {
   double slice_us;            /* propagation time per step before waiting requests join (default 2000) */
   int pass_budget;            /* propagation passes per step (default 0: no limit) */
-  size_t memory_budget_bytes; /* admission limit: the engine's resident bytes plus the device bytes of
-                                 running requests (default 0: no limit) */
+  size_t memory_budget_bytes; /* admission limit on the engine's resident bytes, the server's staging
+                                 buffers and the engine scratch of running requests; idle graphs'
+                                 staging buffers are freed first when a request does not fit
+                                 (default 0: no limit) */
   int max_batches_per_step;   /* new batches started per step (default 0: the engine's max_graphs) */
   int serial;                 /* 1: the plain path, one request at a time run to its end (default 0) */
   int evict_idle;             /* 1: when a request does not fit the budget, graphs with no request
@@ -363,6 +365,9 @@ typedef struct {
 
 /* A server drives one engine; graphs are added to the engine beforehand. */
 int dlp_server_create(dlp_engine *e, const dlp_server_config *cfg, dlp_server **out);
+/* Destroy a server before its engine. Graphs the server evicted to host memory
+ * go back into the engine under their ids (a graph that no longer fits the
+ * engine's budget is dropped and its id released). */
 int dlp_server_destroy(dlp_server *s);
 /* Seconds since the server was created (the clock of dlp_request_result). */
 double dlp_server_clock(const dlp_server *s);

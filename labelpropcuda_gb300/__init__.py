@@ -231,6 +231,8 @@ class Engine:
         self._h = ctypes.c_void_p()
         _n.check(L.dlp_engine_create(ctypes.byref(cfg), max_graphs, memory_budget_bytes, ctypes.byref(self._h)))
         self.sizes: dict[int, int] = {}
+        import weakref
+        self._servers = weakref.WeakSet()  # a server must be destroyed before its engine
 
     @staticmethod
     def graph_bytes(num_nodes: int, num_edges: int, truth: bool = True, batch_map: bool = True,
@@ -352,6 +354,8 @@ class Engine:
 
     def close(self) -> None:
         if self._h:
+            for srv in list(self._servers):
+                srv.close()
             _n.lib().dlp_engine_destroy(self._h)
             self._h = ctypes.c_void_p()
 
@@ -454,6 +458,7 @@ class Server:
         self.engine = engine
         self._h = ctypes.c_void_p()
         _n.check(L.dlp_server_create(engine._h, ctypes.byref(cfg), ctypes.byref(self._h)))
+        engine._servers.add(self)
 
     def reserve(self, gid: int, batches: list[Batch]) -> None:
         """Sizes the graph's buffers for the largest of the given batches."""
@@ -510,8 +515,11 @@ class Server:
         return [_result_dict(out[i]) for i in range(n)], float(span.value)
 
     def close(self) -> None:
+        """Destroys the server (before its engine: destroying restores the
+        graphs it evicted into the engine)."""
         if self._h:
-            _n.lib().dlp_server_destroy(self._h)
+            if self.engine._h:
+                _n.lib().dlp_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

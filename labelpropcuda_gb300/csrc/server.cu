@@ -198,17 +198,34 @@ struct dlp_server {
            dlp_engine_bytes_in_use(eng) + staged_bytes + running_bytes + need <= cfg.memory_budget_bytes;
   }
 
-  // Staging bytes a request adds to its graph's buffer (grow() keeps twice
-  // what it is asked for).
+  // Staging bytes a request adds to its graph's buffer.
   static size_t staging_growth(const GraphBuf &b, const Request &r) {
     const size_t total = std::max<size_t>(r.batch_bytes, 16);
-    return total > b.dev_cap ? 2 * total - b.dev_cap : 0;
+    return total > b.dev_cap ? total - b.dev_cap : 0;
   }
 
-  // Evicts idle resident graphs, least recently used first (never `keep` nor
-  // a graph in `busy`), until `need` more bytes fit. Returns whether they do.
-  int make_room(size_t need, int keep, const std::vector<int> &busy, bool *ok) {
-    *ok = fits(need);
+  // Frees the staging buffers of graphs with no request running that were not
+  // admitted in this round (`busy`); they are only a cache of earlier sizes.
+  void free_idle_staging(const std::vector<int> &busy) {
+    for (size_t g = 0; g < bufs.size(); ++g) {
+      GraphBuf &b = bufs[g];
+      if (!b.dev || b.running >= 0) continue;
+      if (std::find(busy.begin(), busy.end(), static_cast<int>(g)) != busy.end()) continue;
+      free_staging(b);
+    }
+  }
+
+  // Makes room for `need()` more bytes: first the staging buffers of idle
+  // graphs go, then (with evict_idle) idle resident graphs are evicted, least
+  // recently used first (never `keep` nor a graph in `busy`). Sets *ok to
+  // whether the bytes fit.
+  template <class Need>
+  int make_room(Need need, int keep, const std::vector<int> &busy, bool *ok) {
+    *ok = fits(need());
+    if (!*ok) {
+      free_idle_staging(busy);
+      *ok = fits(need());
+    }
     while (!*ok && cfg.evict_idle) {
       int victim = -1;
       for (int g = 0; g < static_cast<int>(bufs.size()); ++g) {
@@ -219,7 +236,7 @@ struct dlp_server {
       }
       if (victim < 0) break;
       DLP_TRY(evict(victim));
-      *ok = fits(need);
+      *ok = fits(need());
     }
     return DLP_OK;
   }
@@ -262,8 +279,8 @@ struct dlp_server {
     if (total > b.dev_cap) {
       DLP_CUDA_TRY(cudaStreamSynchronize(s));
       free_staging(b);
-      DLP_CUDA_TRY(cudaMalloc(&b.dev, total * 2));
-      b.dev_cap = total * 2;
+      DLP_CUDA_TRY(cudaMalloc(&b.dev, total));
+      b.dev_cap = total;
       staged_bytes += b.dev_cap;
     }
     return DLP_OK;
@@ -331,7 +348,7 @@ struct dlp_server {
         continue;
       }
       // an evicted graph needs its own bytes back as well
-      const size_t need = r.bytes + staging_growth(b, r) + (b.evicted ? b.graph_bytes : 0);
+      auto need = [&] { return r.bytes + staging_growth(b, r) + (b.evicted ? b.graph_bytes : 0); };
       bool ok = true;
       DLP_TRY(make_room(need, r.gid, gids, &ok));
       if (!ok) {
@@ -465,7 +482,7 @@ int dlp_server_reserve(dlp_server *s, int graph_id, int max_inserted, int max_gt
   b.res_edges = std::max(b.res_edges, max_edges);
   b.res_deleted = std::max(b.res_deleted, max_deleted);
   if (b.evicted) return DLP_OK;  // applied when the graph is restored
-  DLP_TRY(s->grow(b, (total + 1) / 2));  // grow() keeps twice what it is asked for
+  DLP_TRY(s->grow(b, total));
   return dlp_engine_reserve(s->eng, graph_id, max_edges, max_deleted);
 }
 
@@ -505,7 +522,7 @@ int dlp_server_make_resident(dlp_server *s, int graph_id) {
   GraphBuf &b = s->buf(graph_id);
   if (!b.evicted) return DLP_OK;
   bool ok = true;
-  DLP_TRY(s->make_room(b.graph_bytes, graph_id, {}, &ok));
+  DLP_TRY(s->make_room([&] { return b.graph_bytes; }, graph_id, {}, &ok));
   if (!ok) return dlp::fail(DLP_ERR_OUT_OF_MEMORY, "the graph does not fit the memory budget");
   return s->restore(graph_id);
 }
