@@ -102,6 +102,18 @@ float dlp_mean_edge_weight(int64_t num_edges, const int *col_ind, const float *v
 /*    (the per-batch loop of runDynLP, src/dynLP.cu:284-558).                 */
 /* ------------------------------------------------------------------------ */
 
+/* Division in the label updates (propagation and initialisation). IEEE
+ * round-to-nearest is the default and what the CPU oracle computes, bit for
+ * bit. The reference is built with --use_fast_math (Makefile:52), whose `/` is
+ * the CUDA fast division; DLP_ARITH_REFERENCE_FAST_MATH uses that division
+ * too, for results that follow the reference's own binary more closely (its
+ * float-atomic supernode sums still add in a varying order). */
+enum dlp_arithmetic { DLP_ARITH_IEEE = 0, DLP_ARITH_REFERENCE_FAST_MATH = 1 };
+/* The same choice for the reference-layout step launchers below
+ * (dlp_label_initialization, dlp_iterative_propagation and its allocation-free
+ * variant) launched afterwards by this process. */
+int dlp_set_launcher_arithmetic(int arithmetic);
+
 typedef struct dlp_config {
   float tau;             /* sparsification threshold; < 0: mean full-graph edge weight */
   float delta;           /* convergence threshold (> 0) */
@@ -124,6 +136,8 @@ typedef struct dlp_config {
                             many vertices; 0 = 512, at most 1024 (autotuned) */
   int subgrid_entry;     /* sub-grid mode for total frontiers of at most this
                             many; 0 = 2048, at most 4096 (autotuned) */
+  int arithmetic;        /* enum dlp_arithmetic: the division of the label
+                            updates (default DLP_ARITH_IEEE) */
 } dlp_config;
 
 void dlp_config_default(dlp_config *cfg);

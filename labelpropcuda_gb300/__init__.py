@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native as _n
-from ._native import DlpError, SEMANTICS_REF, SEMANTICS_SPEC  # noqa: F401
+from ._native import DlpError, SEMANTICS_REF, SEMANTICS_SPEC, ARITH_IEEE, ARITH_REFERENCE_FAST_MATH  # noqa: F401
 
 __all__ = ["Problem", "Session", "DeviceArray", "DlpError", "SEMANTICS_REF", "SEMANTICS_SPEC",
            "device_count", "batch_map"]
@@ -118,7 +118,7 @@ class Session:
                  tau: float = -1.0, delta: float = 1e-4, max_iterations: int = 100000,
                  semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False, narrow_lanes: int = 0,
                  blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: int = 7,
-                 solo_entry: int = 0, subgrid_entry: int = 0):
+                 solo_entry: int = 0, subgrid_entry: int = 0, arithmetic: int = 0):
         L = _n.lib()
         cfg = _n.Config()
         L.dlp_config_default(ctypes.byref(cfg))
@@ -127,6 +127,7 @@ class Session:
         cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
         cfg.small_frontier_solo = int(small_frontier_solo)
         cfg.solo_entry, cfg.subgrid_entry = int(solo_entry), int(subgrid_entry)
+        cfg.arithmetic = int(arithmetic)
         self._keep = [np.ascontiguousarray(row_ptr, dtype=np.int32), np.ascontiguousarray(col_ind, dtype=np.int32),
                       np.ascontiguousarray(values, dtype=np.float32)]
         tl = None if true_labels is None else np.ascontiguousarray(true_labels, dtype=np.float32)
@@ -219,7 +220,8 @@ class Engine:
     def __init__(self, max_graphs: int, memory_budget_bytes: int = 0, *, tau: float = -1.0, delta: float = 1e-4,
                  max_iterations: int = 100000, semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False,
                  narrow_lanes: int = 0, blocks_per_sm: int = 0, wait_timeout_s: float = 2.0,
-                 small_frontier_solo: int = 7, solo_entry: int = 0, subgrid_entry: int = 0):
+                 small_frontier_solo: int = 7, solo_entry: int = 0, subgrid_entry: int = 0,
+                 arithmetic: int = 0):
         L = _n.lib()
         cfg = _n.Config()
         L.dlp_config_default(ctypes.byref(cfg))
@@ -228,6 +230,7 @@ class Engine:
         cfg.narrow_lanes, cfg.blocks_per_sm, cfg.wait_timeout_s = narrow_lanes, blocks_per_sm, wait_timeout_s
         cfg.small_frontier_solo = int(small_frontier_solo)
         cfg.solo_entry, cfg.subgrid_entry = int(solo_entry), int(subgrid_entry)
+        cfg.arithmetic = int(arithmetic)
         self._h = ctypes.c_void_p()
         _n.check(L.dlp_engine_create(ctypes.byref(cfg), max_graphs, memory_budget_bytes, ctypes.byref(self._h)))
         self.sizes: dict[int, int] = {}

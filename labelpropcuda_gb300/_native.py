@@ -34,7 +34,7 @@ class Config(ctypes.Structure):
         ("semantics", ctypes.c_int), ("device", ctypes.c_int), ("record", ctypes.c_int),
         ("narrow_lanes", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
         ("wait_timeout_s", ctypes.c_double), ("small_frontier_solo", ctypes.c_int),
-        ("solo_entry", ctypes.c_int), ("subgrid_entry", ctypes.c_int),
+        ("solo_entry", ctypes.c_int), ("subgrid_entry", ctypes.c_int), ("arithmetic", ctypes.c_int),
     ]
 
 
@@ -83,6 +83,9 @@ class TuneReport(ctypes.Structure):
         ("subgrid_entry", ctypes.c_int * 32), ("ms", ctypes.c_double * 32),
     ]
 
+
+# enum dlp_arithmetic
+ARITH_IEEE, ARITH_REFERENCE_FAST_MATH = 0, 1
 
 # status codes
 DLP_OK = 0
@@ -193,6 +196,7 @@ _SIGNATURES = {
                                                _P]),
     "dlp_device_count": (_I, [c_int_p]),
     "dlp_device_name": (_I, [_I, ctypes.c_char_p, _I]),
+    "dlp_set_launcher_arithmetic": (_I, [_I]),
     "dlp_set_device": (_I, [_I]),
     "dlp_malloc": (_I, [ctypes.POINTER(_P), ctypes.c_size_t]),
     "dlp_free": (_I, [_P]),

@@ -182,8 +182,16 @@ __device__ __forceinline__ float from_fixed(long long q) {
 
 // New label from the two row sums (src/iterativePropagation.cu:153-168) with an
 // IEEE round-to-nearest division.
-__device__ __forceinline__ float updated_label(float w_all, float w_label, float old) {
-  float nl = (w_all > 1e-10f) ? __fdiv_rn(w_label, w_all) : old;
+// The quotient of a weighted average. Default: IEEE round-to-nearest, the
+// oracle's arithmetic. fast: the CUDA fast division (__fdividef), the division
+// that the reference's -use_fast_math build makes of its `/`
+// (src/iterativePropagation.cu:160, src/labelInitialization.cu:137; Makefile:52).
+__device__ __forceinline__ float quotient(float num, float den, bool fast) {
+  return fast ? __fdividef(num, den) : __fdiv_rn(num, den);
+}
+
+__device__ __forceinline__ float updated_label(float w_all, float w_label, float old, bool fast = false) {
+  float nl = (w_all > 1e-10f) ? quotient(w_label, w_all, fast) : old;
   return fminf(fmaxf(nl, 0.0f), 1.0f);
 }
 

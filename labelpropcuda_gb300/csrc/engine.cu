@@ -388,6 +388,7 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
   args.ectl = e->ectl;
   args.timeout_ns = static_cast<unsigned long long>(to * 1e9);
   args.solo = e->cfg.small_frontier_solo < 0 ? 7 : e->cfg.small_frontier_solo;
+  args.fast_div = e->cfg.arithmetic == DLP_ARITH_REFERENCE_FAST_MATH ? 1 : 0;
   args.solo_entry = e->cfg.solo_entry > 0 ? e->cfg.solo_entry : dlp::engine::kSoloEntryDefault;
   args.sub_entry = e->cfg.subgrid_entry > 0 ? e->cfg.subgrid_entry : dlp::engine::kSubEntryDefault;
   args.pass_budget = opts.pass_budget;
@@ -580,6 +581,8 @@ int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_bu
   const int lanes = cfg.narrow_lanes == 0 ? 8 : cfg.narrow_lanes;
   if (lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "narrow_lanes must be 4, 8, 16 or 32");
+  if (cfg.arithmetic != DLP_ARITH_IEEE && cfg.arithmetic != DLP_ARITH_REFERENCE_FAST_MATH)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "arithmetic must be DLP_ARITH_IEEE or DLP_ARITH_REFERENCE_FAST_MATH");
   if (cfg.solo_entry < 0 || cfg.solo_entry > dlp::engine::kSoloEntryMax || cfg.subgrid_entry < 0 ||
       cfg.subgrid_entry > dlp::engine::kSubEntryMax)
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "solo_entry must be in [0, 1024] and subgrid_entry in [0, 4096]");

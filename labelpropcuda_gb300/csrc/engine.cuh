@@ -68,6 +68,7 @@ struct EngineArgs {
   EngineCtl *ectl;
   unsigned long long timeout_ns;
   int solo;  // bit 0: one-block passes for small frontiers; bit 1: sub-grid passes; bit 2: team passes
+  int fast_div;    // 1: the reference's fast-math division (dlp_config.arithmetic), else IEEE
   int solo_entry;  // total frontier at most this: one-block passes (<= kSoloEntryMax)
   int sub_entry;   // total frontier at most this: sub-grid passes (<= kSubLive)
   int pass_budget;                // propagation passes this launch runs at most (0: no limit)

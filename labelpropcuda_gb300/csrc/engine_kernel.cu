@@ -10,7 +10,9 @@
 //     src/iterativePropagation.cu:126-150). A row of at most 32 entries only
 //     adds +0 at strides 128..32, so a group of G lanes holding slots lane+G*r
 //     reproduces it exactly; longer rows take a warp holding lane+32*j.
-//   * division is IEEE round-to-nearest (__fdiv_rn); built with -fmad=false.
+//   * division is IEEE round-to-nearest (__fdiv_rn; or, with
+//     dlp_config.arithmetic = 1, the reference's fast-math division);
+//     built with -fmad=false.
 //   * supernode weights are exact 32.32 fixed-point sums (order independent).
 #include "engine.cuh"
 
@@ -681,7 +683,7 @@ __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
         const float w0 = from_fixed(s.acc[2 * root]);
         const float w1 = from_fixed(s.acc[2 * root + 1]);
         const float den = w0 + w1;
-        l = den > 1e-10f ? __fdiv_rn(w1, den) : 0.5f;
+        l = den > 1e-10f ? quotient(w1, den, e.fast_div) : 0.5f;
       }
       s.lab0[u] = l;
       s.lab1[u] = l;
@@ -713,8 +715,8 @@ __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
 // before the row's sum is formed, so a row costs three dependent memory round
 // trips (list entry, row, neighbours) before its marks.
 template <int G>
-__device__ __forceinline__ void narrow_row(const DevState &s, const float *src, float *dst, float delta, int u,
-                                           bool valid, int gl, int &len_out, int (&cand)[32 / G + 1],
+__device__ __forceinline__ void narrow_row(const DevState &s, const float *src, float *dst, float delta, bool fast,
+                                           int u, bool valid, int gl, int &len_out, int (&cand)[32 / G + 1],
                                            unsigned &wide_bits) {
   constexpr int R = 32 / G;
   int rs = 0, len = 0;
@@ -761,7 +763,7 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
   }
   int changed = 0;
   if (valid && gl == 0) {
-    const float nl = updated_label(tw, tl, old);
+    const float nl = updated_label(tw, tl, old, fast);
     dst[u] = nl;
     changed = fabsf(nl - old) > delta;
   }
@@ -833,8 +835,8 @@ __device__ __forceinline__ void group_mark(const GV &w, const int (&cand)[32 / G
 
 // One row of any length by a whole warp: 256 slots held as lane + 32*j.
 template <class Mark>
-__device__ __forceinline__ void wide_row(const DevState &s, const float *src, float *dst, float delta, int u,
-                                         int lane, Mark mark) {
+__device__ __forceinline__ void wide_row(const DevState &s, const float *src, float *dst, float delta, bool fast,
+                                         int u, int lane, Mark mark) {
   const int2 ri = s.rowinfo[u];
   const int rs = ri.x;
   const int len = ri.y;
@@ -871,7 +873,7 @@ __device__ __forceinline__ void wide_row(const DevState &s, const float *src, fl
   int changed = 0;
   if (lane == 0) {
     const float old = src[u];
-    const float nl = updated_label(tw, tl, old);
+    const float nl = updated_label(tw, tl, old, fast);
     dst[u] = nl;
     changed = fabsf(nl - old) > delta;
   }
@@ -1059,7 +1061,7 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
       // the engine's, and the pass offset is added at hand-back
       const int g = c.graph[su];
       const float old = c.lab[src][su];
-      const float nl = updated_label(tw, tl, old);
+      const float nl = updated_label(tw, tl, old, e.fast_div);
       c.lab[src ^ 1][su] = nl;
       c.flags[su] |= 3;
       changed = fabsf(nl - old) > e.delta;
@@ -1437,7 +1439,7 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     int len = 0;
     int cand[32 / G + 1];
     unsigned wide_bits = 0;
-    narrow_row<G>(s, src, dst, w.a.delta, u, valid, gl, len, cand, wide_bits);
+    narrow_row<G>(s, src, dst, w.a.delta, e.fast_div, u, valid, gl, len, cand, wide_bits);
     group_mark<G>(w, cand, wide_bits, stamp, nset, gl);
     add_keyed(valid && gl == 0, static_cast<unsigned>(len), &s.bc->aff_edges);
     add_keyed(valid && gl == 0, 1u, &s.bc->front_visits);
@@ -1463,7 +1465,7 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
       }
       frontier_append(w, fresh, first, v, nset);
     };
-    wide_row(s, src, dst, w.a.delta, u, lane, mark);
+    wide_row(s, src, dst, w.a.delta, e.fast_div, u, lane, mark);
     if (lane == 0) {
       atomicAdd(&s.bc->aff_edges, static_cast<unsigned long long>(s.act_len[u]));
       atomicAdd(&s.bc->front_visits, 1ull);

@@ -12,6 +12,7 @@
 // (numSubEdges, numComponents, iterationsUsed), as the reference's int&
 // outputs require.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
@@ -21,6 +22,9 @@
 namespace dlp {
 namespace ref_layout {
 namespace {
+
+// Division of the label updates in the launchers (dlp_set_launcher_arithmetic).
+std::atomic<int> g_launcher_arith{DLP_ARITH_IEEE};
 
 constexpr int kBlock = 256;
 constexpr int kGroup = 8;               // lanes per row in the row walks
@@ -319,7 +323,7 @@ __global__ void init_accumulate(const int *row_ptr, const int *col, const float 
 
 // src/labelInitialization.cu:99-142.
 __global__ void init_labels(float *labels, const int *comp, int num_comp, const int *gt, const long long *acc,
-                            const int *ins, int I, int n) {
+                            const int *ins, int I, int n, int fast_div) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
   for (int i = t; i < I; i += nt) {
     const int u = ins[i];
@@ -332,7 +336,7 @@ __global__ void init_labels(float *labels, const int *comp, int num_comp, const 
     const float w0 = from_fixed(acc[2 * c]);
     const float w1 = from_fixed(acc[2 * c + 1]);
     const float den = w0 + w1;
-    labels[u] = den > 1e-10f ? __fdiv_rn(w1, den) : 0.5f;
+    labels[u] = den > 1e-10f ? quotient(w1, den, fast_div) : 0.5f;
   }
 }
 
@@ -353,6 +357,7 @@ struct PropArgs {
   GridBarrier *bar;
   int *err;
   unsigned long long timeout_ns;
+  int fast_div;        // the division of the label updates (dlp_set_launcher_arithmetic)
 };
 
 // Frontier loop of src/iterativePropagation.cu:274-327 in one cooperative
@@ -421,7 +426,7 @@ __global__ void __launch_bounds__(kBlock) prop_kernel(PropArgs a) {
       int changed = 0;
       if (valid && gl == 0) {
         const float old = src[u];
-        const float nl = updated_label(tw, tl, old);
+        const float nl = updated_label(tw, tl, old, a.fast_div);
         dst[u] = nl;
         changed = fabsf(nl - old) > a.delta;
       }
@@ -443,7 +448,7 @@ __global__ void __launch_bounds__(kBlock) prop_kernel(PropArgs a) {
       int changed = 0;
       if (lane == 0) {
         const float old = src[u];
-        const float nl = updated_label(tw, tl, old);
+        const float nl = updated_label(tw, tl, old, a.fast_div);
         dst[u] = nl;
         changed = fabsf(nl - old) > a.delta;
       }
@@ -646,6 +651,14 @@ int noalloc_scratch(NoAllocScratch **out) {
 
 extern "C" {
 
+int dlp_set_launcher_arithmetic(int arithmetic) {
+  dlp::clear_error();
+  if (arithmetic != DLP_ARITH_IEEE && arithmetic != DLP_ARITH_REFERENCE_FAST_MATH)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "arithmetic must be DLP_ARITH_IEEE or DLP_ARITH_REFERENCE_FAST_MATH");
+  g_launcher_arith.store(arithmetic);
+  return DLP_OK;
+}
+
 int dlp_mark_deletions(int *d_row_ptr, int *d_col_ind, int *d_vertex_status, int *d_is_affected,
                        const int *d_deleted_nodes, int num_deleted, int num_nodes, void *stream) {
   dlp::clear_error();
@@ -798,7 +811,8 @@ int dlp_label_initialization(const int *d_row_ptr, const int *d_col_ind, const f
       d_row_ptr, d_col_ind, d_values, d_component_id, num_components, d_gt_class, d_inserted_nodes, num_inserted,
       num_nodes, acc);
   init_labels<<<grid_for(num_inserted, kBlock), kBlock, 0, s>>>(d_labels, d_component_id, num_components, d_gt_class,
-                                                               acc, d_inserted_nodes, num_inserted, num_nodes);
+                                                               acc, d_inserted_nodes, num_inserted, num_nodes,
+                                                               g_launcher_arith.load());
   DLP_CUDA_TRY(cudaGetLastError());
   DLP_CUDA_TRY(cudaFreeAsync(acc, s));
   return DLP_OK;
@@ -848,6 +862,7 @@ int dlp_iterative_propagation(const int *d_row_ptr, const int *d_col_ind, const 
   a.err = small + 12;
   a.bar = bar;
   a.timeout_ns = 2000000000ull;
+  a.fast_div = g_launcher_arith.load();
   const void *kern = prop_kernel_ptr(8);
   const int grid = coop_grid(kern);
   if (grid <= 0) return dlp::fail(DLP_ERR_CUDA, "occupancy query failed");
@@ -917,6 +932,7 @@ int dlp_iterative_propagation_noalloc(const int *d_row_ptr, const int *d_col_ind
   a.err = sc->small + 12;
   a.bar = &sc->bar;
   a.timeout_ns = 2000000000ull;
+  a.fast_div = g_launcher_arith.load();
   const void *kern = prop_kernel_ptr(8);
   const int grid = coop_grid(kern);
   if (grid <= 0) return dlp::fail(DLP_ERR_CUDA, "occupancy query failed");

@@ -297,9 +297,15 @@ def read_ref_dump(path: Path) -> dict:
     for _ in range(nb):
         head = np.frombuffer(buf, np.int32, 5, off)
         off += 20
-        batches.append({"num_new_edges": int(head[0]), "num_sub_edges": int(head[1]), "hook_edges": int(head[2]),
-                        "num_components": int(head[3]), "iterations": int(head[4]),
-                        "comp_id": vec(np.int32), "init_labels": vec(np.float32),
-                        "seed_marks": vec(np.int32), "labels": vec(np.float32)})
+        rec = {"num_new_edges": int(head[0]), "num_sub_edges": int(head[1]), "hook_edges": int(head[2]),
+               "num_components": int(head[3]), "iterations": int(head[4]),
+               "comp_id": vec(np.int32), "init_labels": vec(np.float32),
+               "seed_marks": vec(np.int32), "labels": vec(np.float32)}
+        # the propagation launcher's inputs (empty unless recorded)
+        for name, dt in (("in_row_ptr", np.int32), ("in_col_ind", np.int32), ("in_values", np.float32),
+                         ("in_labels", np.float32), ("in_status", np.int32), ("in_gt", np.int32),
+                         ("in_affected", np.int32)):
+            rec[name] = vec(dt)
+        batches.append(rec)
     return {"n": n, "record": bool(record), "tau": tau, "batches": batches, "batch_ms": vec(np.float32),
             "accuracy": vec(np.float32), "final_labels": vec(np.float32)}

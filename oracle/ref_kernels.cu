@@ -17,8 +17,9 @@
 //   launchBuildSparsifiedSubgraph  numNewEdges, numSubEdges, tau
 //   launchConnectedComponents      numComponents, component id per inserted vertex
 //   launchLabelInitialization      label per inserted vertex after the step
-//   launchIterativePropagation     affected flags on entry, iterationsUsed,
-//                                  labels on exit
+//   launchIterativePropagation     its inputs (active CSR, labels, status,
+//                                  ground-truth classes, affected flags),
+//                                  iterationsUsed, labels on exit
 // One pass-through changes an argument: the components step is given
 // min(numSubEdges, numNewEdges) edges, because the reference reads
 // numSubEdges entries of an edge list of numNewEdges (src/dynLP.cu:437-440)
@@ -75,6 +76,10 @@ struct BatchRecord {
   std::vector<float> init_labels; // per inserted position (-1 entries absent: step did not run)
   std::vector<int> seed_marks;    // vertices flagged affected when propagation starts
   std::vector<float> labels;      // all vertices after propagation
+  // everything propagation starts from (its launcher's inputs), so that
+  // another propagation can be run from exactly the same state
+  std::vector<int> in_row_ptr, in_col_ind, in_status, in_gt, in_affected;
+  std::vector<float> in_values, in_labels;
 };
 
 bool g_record = false;
@@ -168,6 +173,14 @@ void launchIterativePropagation(const int *d_rowPtr, const int *d_colInd, const 
     const std::vector<int> aff = fetch(d_isAffected, numNodes, stream);
     for (int v = 0; v < numNodes; ++v)
       if (aff[v]) g_cur.seed_marks.push_back(v);
+    g_cur.in_row_ptr = fetch(d_rowPtr, static_cast<size_t>(numNodes) + 1, stream);
+    const size_t m = static_cast<size_t>(g_cur.in_row_ptr[numNodes]);
+    g_cur.in_col_ind = fetch(d_colInd, m, stream);
+    g_cur.in_values = fetch(d_values, m, stream);
+    g_cur.in_labels = fetch(static_cast<const float *>(d_labels), numNodes, stream);
+    g_cur.in_status = fetch(d_vertexStatus, numNodes, stream);
+    g_cur.in_gt = fetch(d_gtClass, numNodes, stream);
+    g_cur.in_affected = aff;
   }
   ref_launchIterativePropagation(d_rowPtr, d_colInd, d_values, d_labels, d_labelsBuffer, d_vertexStatus, d_gtClass,
                                  d_isAffected, numNodes, delta, maxIterations, iterationsUsed, stream);
@@ -216,6 +229,13 @@ int main(int argc, char **argv) {
     put_vec(f, r.init_labels);
     put_vec(f, r.seed_marks);
     put_vec(f, r.labels);
+    put_vec(f, r.in_row_ptr);
+    put_vec(f, r.in_col_ind);
+    put_vec(f, r.in_values);
+    put_vec(f, r.in_labels);
+    put_vec(f, r.in_status);
+    put_vec(f, r.in_gt);
+    put_vec(f, r.in_affected);
   }
   put_vec(f, times);
   put_vec(f, accuracy);
