@@ -588,20 +588,37 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     warm = [p.batches[:skip] for p in probs]  # applied untimed before every measured phase
     for p in probs:  # the requests of this run: batches skip .. skip+nb-1 of each graph
         p.batches = p.batches[skip:skip + nb]
-    for g, p, w in zip(gids, probs, warm):  # scratch sized up front: no allocation inside the timed runs
-        eng.reserve(g, max(bt.edge_src.size for bt in p.batches + w), max(bt.deleted.size for bt in p.batches + w))
     packed = [PackedBatches([p.batches[b] for p in probs]) for b in range(nb)]
     setup_s = time.perf_counter() - t_setup
     progress(f"served setup {setup_s:.1f} s: {len(probs)} graphs, lanes {lanes}, blocks/SM {bps or 'occupancy'}")
     vertices = sum(p.num_nodes for p in probs)
     edges_full = sum(p.num_edges for p in probs)
 
+    snaps = None  # the graphs' state after the warm-up batches, in host memory
+
+    def reserve_all():
+        for g, p, w in zip(gids, probs, warm):  # scratch sized up front: no allocation inside the timed runs
+            eng.reserve(g, max(bt.edge_src.size for bt in p.batches + w), max(bt.deleted.size for bt in p.batches + w))
+
     def reset_all():
+        nonlocal snaps
+        if snaps is not None:  # back to the warmed-up state without replaying the warm-up
+            for g, sn in zip(gids, snaps):
+                eng.remove_graph(g)
+                eng.restore_as(sn, g)
+            reserve_all()
+            eng.synchronize()
+            return
         for g in gids:
             eng.reset_graph(g)
         for b in range(skip):  # the graphs' state before the served batches (untimed)
             eng.step([(g, b, w[b]) for g, w in zip(gids, warm)], wait=False)
         eng.synchronize()
+        if skip > 0:
+            snaps = [eng.snapshot(g) for g in gids]
+            progress(f"warm state: {sum(len(x) for x in snaps) / 1e9:.1f} GB snapshotted to host memory")
+
+    reserve_all()
 
     # batched: one launch per step over every graph
     def batched_run():

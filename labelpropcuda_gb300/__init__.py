@@ -283,6 +283,11 @@ class Engine:
         self.sizes[gid.value] = int(_n.lib().dlp_engine_graph_nodes(self._h, gid.value))
         return gid.value
 
+    def restore_as(self, snap: bytes, gid: int) -> None:
+        """Makes a snapshotted graph resident again under the given free id."""
+        _n.check(_n.lib().dlp_engine_restore_as(self._h, snap, len(snap), gid))
+        self.sizes[gid] = int(_n.lib().dlp_engine_graph_nodes(self._h, gid))
+
     def tau(self, gid: int) -> float:
         return float(_n.lib().dlp_engine_tau(self._h, gid))
 

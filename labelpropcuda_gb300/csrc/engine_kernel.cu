@@ -278,7 +278,7 @@ __device__ void phase_a(const EngineArgs &e, const Ctx &c, int *pref) {
     i -= a.E;
     const int cb = s.ctl->cur_buf;
     const int v = s.touched[static_cast<size_t>((a.seq - 1) & 1) * n + i];
-    (cb ? s.lab0 : s.lab1)[v] = (cb ? s.lab1 : s.lab0)[v];
+    s.vrec[v].lab[cb ^ 1] = s.vrec[v].lab[cb];
   }
   for (int g = c.gtid; g < ng; g += c.nthreads) {
     const GraphRec &r = e.recs[g];
@@ -319,9 +319,9 @@ __device__ void phase_b(const EngineArgs &e, const Ctx &c, int *pref) {
     const int v = a.gt_ids[i];
     const float l = a.gt_lab[i];
     s.gt[v] = l < 0.5f ? 0 : 1;
-    s.nmeta[v] = s.act_len[v] > kNarrowMax ? 2 : 0;  // not markable any more
-    s.lab0[v] = l;
-    s.lab1[v] = l;
+    s.vrec[v].meta = s.act_len[v] > kNarrowMax ? 2u : 0u;  // not markable any more
+    s.vrec[v].lab[0] = l;
+    s.vrec[v].lab[1] = l;
     if (!(a.spec && s.del_stamp[v] == w.cur)) s.status[v] = kGroundTruth;
   }
   // Rows whose live content can change: every changed vertex and its
@@ -403,7 +403,7 @@ __device__ void phase_c(const EngineArgs &e, const Ctx &c, int *pref) {
       const int len = keep_row ? pos : 0;
       s.act_len[u] = len;
       s.rowinfo[u] = make_int2(rs, len);
-      s.nmeta[u] = static_cast<uint8_t>((s.gt[u] < 0 ? 1 : 0) | (len > kNarrowMax ? 2 : 0));
+      s.vrec[u].meta = (s.gt[u] < 0 ? 1u : 0u) | (len > kNarrowMax ? 2u : 0u);
     }
   });
 
@@ -685,16 +685,16 @@ __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
         const float den = w0 + w1;
         l = den > 1e-10f ? quotient(w1, den, e.fast_div) : 0.5f;
       }
-      s.lab0[u] = l;
-      s.lab1[u] = l;
+      s.vrec[u].lab[0] = l;
+      s.vrec[u].lab[1] = l;
     } else if (s.gt_stamp[u] == w.cur && s.gt[u] >= 0) {
       // new vertices without new edges (src/dynLP.cu:482-504): this batch's
       // ground truth keeps the label set in phase B, everything else 0.5
-      l = s.lab0[u];
+      l = s.vrec[u].lab[0];
     } else {
       l = 0.5f;
-      s.lab0[u] = l;
-      s.lab1[u] = l;
+      s.vrec[u].lab[0] = l;
+      s.vrec[u].lab[1] = l;
     }
     if (a.record) {
       s.rec_init[i] = l;
@@ -715,9 +715,8 @@ __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
 // before the row's sum is formed, so a row costs three dependent memory round
 // trips (list entry, row, neighbours) before its marks.
 template <int G>
-__device__ __forceinline__ void narrow_row(const DevState &s, const float *src, float *dst, float delta, bool fast,
-                                           int u, bool valid, int gl, int &len_out, int (&cand)[32 / G + 1],
-                                           unsigned &wide_bits) {
+__device__ __forceinline__ void narrow_row(const DevState &s, int sb, float delta, bool fast, int u, bool valid,
+                                           int gl, int &len_out, int (&cand)[32 / G + 1], unsigned &wide_bits) {
   constexpr int R = 32 / G;
   int rs = 0, len = 0;
   float old = 0.0f;
@@ -725,7 +724,7 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
     const int2 ri = s.rowinfo[u];
     rs = ri.x;
     len = ri.y;
-    if (gl == 0) old = src[u];
+    if (gl == 0) old = s.vrec[u].lab[sb];
   }
   float sw[R], sl[R];
   int vv[R];
@@ -740,11 +739,12 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
       const int2 ent = s.act_adj[rs + ee];
       if (ent.x >= 0) {
         const float wt = __int_as_float(ent.y);
-        sw[r] = wt;                               // 0 + w
-        sl[r] = __fmaf_rn(wt, src[ent.x], 0.0f);  // fma(w, F_v, 0)
-        const unsigned meta = s.nmeta[ent.x];
-        if (meta & 1u) vv[r] = ent.x;
-        if (meta & 2u) wb |= 1u << r;
+        // the neighbour's label and metadata: one 16-byte load, one sector
+        const uint4 nb = *reinterpret_cast<const uint4 *>(&s.vrec[ent.x]);
+        sw[r] = wt;                                                           // 0 + w
+        sl[r] = __fmaf_rn(wt, __uint_as_float(sb ? nb.y : nb.x), 0.0f);  // fma(w, F_v, 0)
+        if (nb.z & 1u) vv[r] = ent.x;
+        if (nb.z & 2u) wb |= 1u << r;
       }
     }
   }
@@ -764,7 +764,7 @@ __device__ __forceinline__ void narrow_row(const DevState &s, const float *src, 
   int changed = 0;
   if (valid && gl == 0) {
     const float nl = updated_label(tw, tl, old, fast);
-    dst[u] = nl;
+    s.vrec[u].lab[sb ^ 1] = nl;
     changed = fabsf(nl - old) > delta;
   }
   changed = __shfl_sync(0xffffffffu, changed, 0, G);
@@ -835,8 +835,8 @@ __device__ __forceinline__ void group_mark(const GV &w, const int (&cand)[32 / G
 
 // One row of any length by a whole warp: 256 slots held as lane + 32*j.
 template <class Mark>
-__device__ __forceinline__ void wide_row(const DevState &s, const float *src, float *dst, float delta, bool fast,
-                                         int u, int lane, Mark mark) {
+__device__ __forceinline__ void wide_row(const DevState &s, int sb, float delta, bool fast, int u, int lane,
+                                         Mark mark) {
   const int2 ri = s.rowinfo[u];
   const int rs = ri.x;
   const int len = ri.y;
@@ -852,7 +852,7 @@ __device__ __forceinline__ void wide_row(const DevState &s, const float *src, fl
         if (ent.x >= 0) {
           const float wt = __int_as_float(ent.y);
           sw[j] = sw[j] + wt;
-          sl[j] = __fmaf_rn(wt, src[ent.x], sl[j]);
+          sl[j] = __fmaf_rn(wt, s.vrec[ent.x].lab[sb], sl[j]);
         }
       }
     }
@@ -872,9 +872,9 @@ __device__ __forceinline__ void wide_row(const DevState &s, const float *src, fl
   }
   int changed = 0;
   if (lane == 0) {
-    const float old = src[u];
+    const float old = s.vrec[u].lab[sb];
     const float nl = updated_label(tw, tl, old, fast);
-    dst[u] = nl;
+    s.vrec[u].lab[sb ^ 1] = nl;
     changed = fabsf(nl - old) > delta;
   }
   changed = __shfl_sync(0xffffffffu, changed, 0);
@@ -985,8 +985,9 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
     const unsigned long long prev = atomicCAS(&c.key[h], kEmptyKey, key);
     if (prev == kEmptyKey) {
       const DevState &s = e.recs[g].st;
-      c.lab[0][h] = s.lab0[v];
-      c.lab[1][h] = s.lab1[v];
+      const float2 both = *reinterpret_cast<const float2 *>(s.vrec[v].lab);
+      c.lab[0][h] = both.x;
+      c.lab[1][h] = both.y;
       c.gt[h] = s.gt[v];
       const int len = s.act_len[v];
       c.len[h] = len > kNarrowMax ? kWideLen : static_cast<unsigned char>(len);
@@ -1356,8 +1357,7 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     }
     if (!(c.flags[i] & 1)) continue;
     const int v = static_cast<int>(c.key[i] & 0xffffffffu);
-    s.lab0[v] = c.lab[0][i];
-    s.lab1[v] = c.lab[1][i];
+    *reinterpret_cast<float2 *>(s.vrec[v].lab) = make_float2(c.lab[0][i], c.lab[1][i]);
   }
   // per-graph pass counts, and the frontier back into the set of the graph's
   // pass k + pass0 (the set after it empty)
@@ -1431,15 +1431,13 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     const DevState &s = w.s;
     const int kg = k + w.a.pass0;
     const int nset = (kg + 1) % 3;
-    const int cb = s.ctl->cur_buf;
-    const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
-    float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
+    const int sb = (s.ctl->cur_buf ^ kg) & 1;  // the buffer pass kg reads
     const unsigned stamp = w.g0 + static_cast<unsigned>(kg) + 1u;
     const int u = valid ? s.flist[static_cast<size_t>(kg % 3) * s.n + (item - pref[g])] : 0;
     int len = 0;
     int cand[32 / G + 1];
     unsigned wide_bits = 0;
-    narrow_row<G>(s, src, dst, w.a.delta, e.fast_div, u, valid, gl, len, cand, wide_bits);
+    narrow_row<G>(s, sb, w.a.delta, e.fast_div, u, valid, gl, len, cand, wide_bits);
     group_mark<G>(w, cand, wide_bits, stamp, nset, gl);
     add_keyed(valid && gl == 0, static_cast<unsigned>(len), &s.bc->aff_edges);
     add_keyed(valid && gl == 0, 1u, &s.bc->front_visits);
@@ -1451,9 +1449,7 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     const DevState &s = w.s;
     const int kg = k + w.a.pass0;
     const int nset = (kg + 1) % 3;
-    const int cb = s.ctl->cur_buf;
-    const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
-    float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
+    const int sb = (s.ctl->cur_buf ^ kg) & 1;
     const unsigned stamp = w.g0 + static_cast<unsigned>(kg) + 1u;
     const int u = s.flist[static_cast<size_t>(kg % 3) * s.n + (s.n - 1 - (wi - pref2[g]))];
     auto mark = [&](bool cand, int v) {
@@ -1465,7 +1461,7 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
       }
       frontier_append(w, fresh, first, v, nset);
     };
-    wide_row(s, src, dst, w.a.delta, e.fast_div, u, lane, mark);
+    wide_row(s, sb, w.a.delta, e.fast_div, u, lane, mark);
     if (lane == 0) {
       atomicAdd(&s.bc->aff_edges, static_cast<unsigned long long>(s.act_len[u]));
       atomicAdd(&s.bc->front_visits, 1ull);
@@ -1590,8 +1586,7 @@ __device__ void phase_h(const EngineArgs &e, const Ctx &c, int *pref, int k_end)
       if (i < a.G) {
         const int v = a.gt_ids[i];
         const float l = s.gt[v] == 0 ? 0.0f : 1.0f;
-        s.lab0[v] = l;
-        s.lab1[v] = l;
+        *reinterpret_cast<float2 *>(s.vrec[v].lab) = make_float2(l, l);
       } else if ((i -= a.G) < a.D) {
         s.del_keep[i] = a.del[i];  // the next batch restores these rows (ref)
       } else {
@@ -1606,8 +1601,7 @@ __device__ void phase_h(const EngineArgs &e, const Ctx &c, int *pref, int k_end)
         int now = -1;
         if (st != kDeleted && st != kGroundTruth) {
           const int passes = s.bc->passes;
-          const float *lab = ((s.ctl->cur_buf ^ passes) & 1) ? s.lab1 : s.lab0;
-          const int pred = lab[v] >= 0.5f ? 1 : 0;
+          const int pred = s.vrec[v].lab[(s.ctl->cur_buf ^ passes) & 1] >= 0.5f ? 1 : 0;
           const int truth = s.truth ? s.truth[v] : 0;
           now = pred == truth ? 1 : 0;
         }
