@@ -149,7 +149,9 @@ typedef struct dlp_batch_stats {
   int num_components;      /* connected components among inserted vertices */
   int num_sub_edges;       /* 2 x new-new edges with w > tau (numSubEdges) */
   int hook_edges;          /* edges hooked by the components step */
-  int hook_rounds;         /* hook passes until no change */
+  int hook_rounds;         /* hook passes until no change; hooks of one pass race (as in the
+                              reference), so this count can vary from run to run while the
+                              components themselves do not */
   int seed_frontier;       /* |F_0| */
   int seed_marks;          /* vertices marked affected before filtering */
   int64_t affected_edges;  /* sum over passes of the frontier's row lengths */

@@ -14,7 +14,7 @@ import pytest
 import labelpropcuda_gb300 as dlp
 from labelpropcuda_gb300 import _native as N
 
-EXACT = ["iterations", "num_components", "num_sub_edges", "hook_edges", "hook_rounds", "seed_frontier",
+EXACT = ["iterations", "num_components", "num_sub_edges", "hook_edges", "seed_frontier",
          "seed_marks", "affected_edges", "frontier_visits", "correct", "total", "init_branch", "hook_truncated",
          "dirty_rows", "dirty_entries"]
 

@@ -24,7 +24,7 @@ import pytest
 
 import labelpropcuda_gb300 as dlp
 
-EXACT = ["iterations", "num_components", "num_sub_edges", "hook_edges", "hook_rounds", "seed_frontier",
+EXACT = ["iterations", "num_components", "num_sub_edges", "hook_edges", "seed_frontier",
          "seed_marks", "affected_edges", "frontier_visits", "correct", "total", "init_branch", "hook_truncated",
          "dirty_rows", "dirty_entries"]
 BATCHES = 3
