@@ -469,6 +469,9 @@ def gpu_arm(args, td, rank, world, local_rank):
         "clocks": clocks,
         "gpu_launches": args.steps * nb * 2,
     }
+    if args.per_batch:
+        line["per_batch"] = [{k: s[k] for k in ("batch", "iterations", "affected_edges", "frontier_visits",
+                                                 "dirty_entries", "device_ms")} for s in stats0]
     if served is not None:
         line["served"] = served
     print(json.dumps(line), flush=True)
@@ -826,6 +829,7 @@ def main(argv=None) -> int:
     ap.add_argument("--plain-per-stratum", type=int, default=3)
     ap.add_argument("--plain-strata", type=int, default=8)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 oracle error of the headline workload")
+    ap.add_argument("--per-batch", action="store_true", help="add every batch's statistics to the line")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's own CUDA build (oracle/_ref/ref_kernels)")
     args = ap.parse_args(argv)

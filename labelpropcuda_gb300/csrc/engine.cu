@@ -7,9 +7,7 @@
 //   act_adj   int2[m]        live rows in the same slots as full_adj
 //   act_len   int32[n]       live row length
 //   status/gt int8[n]        truth uint8[n]       contrib int32[n]
-//   vrec      16 B[n]        {label buffer 0, label buffer 1, neighbour metadata, -}:
-//                            the stale double buffer of the reference, and what a
-//                            pass needs about a neighbour, in one 32-byte sector
+//   lab0/lab1 fp32[n]        the stale double buffer of the reference
 //   stamps    uint32[n] x 4  (deleted, ground truth, dirty, frontier)
 //   lists     int32: dirty[n], seeds[n], frontier 3 x [n], touched 2 x [n]
 //   SV        par int32[n], acc int64[2n]
@@ -47,11 +45,10 @@ __global__ void rowinfo_reset_kernel(const int *full_row, int2 *rowinfo, int64_t
     rowinfo[i] = make_int2(full_row[i], 0);
 }
 
-// Every vertex record to {0.5, 0.5} with metadata 1: no ground truth, empty row.
-__global__ void vrec_reset_kernel(dlp::session::VRec *r, int64_t count) {
+__global__ void fill_f32_kernel(float *p, float v, int64_t count) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    *reinterpret_cast<uint4 *>(&r[i]) = make_uint4(__float_as_uint(0.5f), __float_as_uint(0.5f), 1u, 0u);
+    p[i] = v;
 }
 
 size_t align16(size_t x) { return (x + 15) & ~static_cast<size_t>(15); }
@@ -249,12 +246,14 @@ int reset_graph(dlp_engine *e, GraphSlot *g, int gid) {
   DLP_CUDA_TRY(cudaMemsetAsync(d.act_len, 0, sizeof(int) * n, q));
   DLP_CUDA_TRY(cudaMemsetAsync(d.status, dlp::kDeleted, n, q));
   DLP_CUDA_TRY(cudaMemsetAsync(d.gt, 0xff, n, q));
+  DLP_CUDA_TRY(cudaMemsetAsync(d.nmeta, 1, n, q));  // no ground truth, empty rows
   DLP_CUDA_TRY(cudaMemsetAsync(d.contrib, 0xff, sizeof(int) * n, q));
   DLP_CUDA_TRY(cudaMemsetAsync(d.local, 0xff, sizeof(int) * n, q));
   for (unsigned *p : {d.del_stamp, d.gt_stamp, d.dirty_stamp, d.front_stamp})
     DLP_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(unsigned) * n, q));
   rowinfo_reset_kernel<<<1024, 256, 0, q>>>(d.full_row, d.rowinfo, n);
-  vrec_reset_kernel<<<1024, 256, 0, q>>>(d.vrec, n);
+  fill_f32_kernel<<<1024, 256, 0, q>>>(d.lab0, 0.5f, n);
+  fill_f32_kernel<<<1024, 256, 0, q>>>(d.lab1, 0.5f, n);
   DLP_CUDA_TRY(cudaGetLastError());
   DLP_CUDA_TRY(cudaMemsetAsync(e->ctl_all + gid, 0, sizeof(SessionCtl), q));
   DLP_CUDA_TRY(cudaStreamSynchronize(q));
@@ -388,7 +387,7 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
   args.ng_new = count;
   args.ectl = e->ectl;
   args.timeout_ns = static_cast<unsigned long long>(to * 1e9);
-  args.solo = e->cfg.small_frontier_solo < 0 ? 7 : e->cfg.small_frontier_solo;
+  args.solo = e->cfg.small_frontier_solo < 0 ? 15 : e->cfg.small_frontier_solo;
   args.fast_div = e->cfg.arithmetic == DLP_ARITH_REFERENCE_FAST_MATH ? 1 : 0;
   args.solo_entry = e->cfg.solo_entry > 0 ? e->cfg.solo_entry : dlp::engine::kSoloEntryDefault;
   args.sub_entry = e->cfg.subgrid_entry > 0 ? e->cfg.subgrid_entry : dlp::engine::kSubEntryDefault;
@@ -521,15 +520,15 @@ int alloc_graph(dlp_engine *e, int n, int64_t m, bool with_truth, bool with_bmap
   if ((st = dalloc(&full_row, n + 1, o, b, z)) || (st = dalloc(&full_adj, m, o, b, z)) ||
       (st = dalloc(&d.act_adj, m, o, b, z)) || (st = dalloc(&d.act_len, n, o, b, z)) ||
       (st = dalloc(&d.status, n, o, b, z)) || (st = dalloc(&d.gt, n, o, b, z)) ||
-      (st = dalloc(&d.contrib, n, o, b, z)) || (st = dalloc(&d.vrec, n, o, b, z)) ||
-      (st = dalloc(&d.local, n, o, b, z)) ||
+      (st = dalloc(&d.contrib, n, o, b, z)) || (st = dalloc(&d.lab0, n, o, b, z)) ||
+      (st = dalloc(&d.lab1, n, o, b, z)) || (st = dalloc(&d.local, n, o, b, z)) ||
       (st = dalloc(&d.del_stamp, n, o, b, z)) || (st = dalloc(&d.gt_stamp, n, o, b, z)) ||
       (st = dalloc(&d.dirty_stamp, n, o, b, z)) || (st = dalloc(&d.front_stamp, n, o, b, z)) ||
       (st = dalloc(&d.dirty_list, n, o, b, z)) || (st = dalloc(&d.seed_list, n, o, b, z)) ||
       (st = dalloc(&d.flist, 3 * static_cast<size_t>(n), o, b, z)) ||
       (st = dalloc(&d.touched, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&d.par, n, o, b, z)) ||
       (st = dalloc(&d.acc, 2 * static_cast<size_t>(n), o, b, z)) || (st = dalloc(&g->stats, kStepRing, o, b, z)) ||
-      (st = dalloc(&d.rowinfo, n, o, b, z)) ||
+      (st = dalloc(&d.nmeta, n, o, b, z)) || (st = dalloc(&d.rowinfo, n, o, b, z)) ||
       (with_truth && (st = dalloc(&truth, n, o, b, z))) || (with_bmap && (st = dalloc(&bmap, n, o, b, z))) ||
       (e->cfg.record &&
        ((st = dalloc(&d.rec_front0, n, o, b, z)) || (st = dalloc(&d.rec_root, n, o, b, z)) ||
@@ -566,7 +565,7 @@ void dlp_config_default(dlp_config *cfg) {
   cfg->max_iterations = 100000;
   cfg->semantics = DLP_SEMANTICS_REF;
   cfg->wait_timeout_s = 2.0;
-  cfg->small_frontier_solo = 7;
+  cfg->small_frontier_solo = 15;
 }
 
 int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_budget_bytes, dlp_engine **out) {
@@ -1072,9 +1071,7 @@ int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels) {
   DLP_TRY(dlp_engine_synchronize(e));
   int cb = 0;
   DLP_CUDA_TRY(cudaMemcpy(&cb, &e->ctl_all[graph_id].cur_buf, sizeof(int), cudaMemcpyDeviceToHost));
-  // the current buffer's field of every vertex record (16-byte pitch)
-  DLP_CUDA_TRY(cudaMemcpy2D(host_labels, sizeof(float), &g->st.vrec[0].lab[cb & 1], sizeof(dlp::session::VRec),
-                            sizeof(float), g->n, cudaMemcpyDeviceToHost));
+  DLP_CUDA_TRY(cudaMemcpy(host_labels, cb ? g->st.lab1 : g->st.lab0, sizeof(float) * g->n, cudaMemcpyDeviceToHost));
   return DLP_OK;
 }
 

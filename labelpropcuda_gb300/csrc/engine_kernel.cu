@@ -278,7 +278,7 @@ __device__ void phase_a(const EngineArgs &e, const Ctx &c, int *pref) {
     i -= a.E;
     const int cb = s.ctl->cur_buf;
     const int v = s.touched[static_cast<size_t>((a.seq - 1) & 1) * n + i];
-    s.vrec[v].lab[cb ^ 1] = s.vrec[v].lab[cb];
+    (cb ? s.lab0 : s.lab1)[v] = (cb ? s.lab1 : s.lab0)[v];
   }
   for (int g = c.gtid; g < ng; g += c.nthreads) {
     const GraphRec &r = e.recs[g];
@@ -319,9 +319,9 @@ __device__ void phase_b(const EngineArgs &e, const Ctx &c, int *pref) {
     const int v = a.gt_ids[i];
     const float l = a.gt_lab[i];
     s.gt[v] = l < 0.5f ? 0 : 1;
-    s.vrec[v].meta = s.act_len[v] > kNarrowMax ? 2u : 0u;  // not markable any more
-    s.vrec[v].lab[0] = l;
-    s.vrec[v].lab[1] = l;
+    s.nmeta[v] = s.act_len[v] > kNarrowMax ? 2 : 0;  // not markable any more
+    s.lab0[v] = l;
+    s.lab1[v] = l;
     if (!(a.spec && s.del_stamp[v] == w.cur)) s.status[v] = kGroundTruth;
   }
   // Rows whose live content can change: every changed vertex and its
@@ -403,7 +403,7 @@ __device__ void phase_c(const EngineArgs &e, const Ctx &c, int *pref) {
       const int len = keep_row ? pos : 0;
       s.act_len[u] = len;
       s.rowinfo[u] = make_int2(rs, len);
-      s.vrec[u].meta = (s.gt[u] < 0 ? 1u : 0u) | (len > kNarrowMax ? 2u : 0u);
+      s.nmeta[u] = static_cast<uint8_t>((s.gt[u] < 0 ? 1 : 0) | (len > kNarrowMax ? 2 : 0));
     }
   });
 
@@ -685,16 +685,16 @@ __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
         const float den = w0 + w1;
         l = den > 1e-10f ? quotient(w1, den, e.fast_div) : 0.5f;
       }
-      s.vrec[u].lab[0] = l;
-      s.vrec[u].lab[1] = l;
+      s.lab0[u] = l;
+      s.lab1[u] = l;
     } else if (s.gt_stamp[u] == w.cur && s.gt[u] >= 0) {
       // new vertices without new edges (src/dynLP.cu:482-504): this batch's
       // ground truth keeps the label set in phase B, everything else 0.5
-      l = s.vrec[u].lab[0];
+      l = s.lab0[u];
     } else {
       l = 0.5f;
-      s.vrec[u].lab[0] = l;
-      s.vrec[u].lab[1] = l;
+      s.lab0[u] = l;
+      s.lab1[u] = l;
     }
     if (a.record) {
       s.rec_init[i] = l;
@@ -715,8 +715,9 @@ __device__ void phase_f(const EngineArgs &e, const Ctx &c, int *pref) {
 // before the row's sum is formed, so a row costs three dependent memory round
 // trips (list entry, row, neighbours) before its marks.
 template <int G>
-__device__ __forceinline__ void narrow_row(const DevState &s, int sb, float delta, bool fast, int u, bool valid,
-                                           int gl, int &len_out, int (&cand)[32 / G + 1], unsigned &wide_bits) {
+__device__ __forceinline__ void narrow_row(const DevState &s, const float *src, float *dst, float delta, bool fast,
+                                           int u, bool valid, int gl, int &len_out, int (&cand)[32 / G + 1],
+                                           unsigned &wide_bits) {
   constexpr int R = 32 / G;
   int rs = 0, len = 0;
   float old = 0.0f;
@@ -724,7 +725,7 @@ __device__ __forceinline__ void narrow_row(const DevState &s, int sb, float delt
     const int2 ri = s.rowinfo[u];
     rs = ri.x;
     len = ri.y;
-    if (gl == 0) old = s.vrec[u].lab[sb];
+    if (gl == 0) old = src[u];
   }
   float sw[R], sl[R];
   int vv[R];
@@ -739,12 +740,11 @@ __device__ __forceinline__ void narrow_row(const DevState &s, int sb, float delt
       const int2 ent = s.act_adj[rs + ee];
       if (ent.x >= 0) {
         const float wt = __int_as_float(ent.y);
-        // the neighbour's label and metadata: one 16-byte load, one sector
-        const uint4 nb = *reinterpret_cast<const uint4 *>(&s.vrec[ent.x]);
-        sw[r] = wt;                                                           // 0 + w
-        sl[r] = __fmaf_rn(wt, __uint_as_float(sb ? nb.y : nb.x), 0.0f);  // fma(w, F_v, 0)
-        if (nb.z & 1u) vv[r] = ent.x;
-        if (nb.z & 2u) wb |= 1u << r;
+        sw[r] = wt;                               // 0 + w
+        sl[r] = __fmaf_rn(wt, src[ent.x], 0.0f);  // fma(w, F_v, 0)
+        const unsigned meta = s.nmeta[ent.x];
+        if (meta & 1u) vv[r] = ent.x;
+        if (meta & 2u) wb |= 1u << r;
       }
     }
   }
@@ -764,7 +764,7 @@ __device__ __forceinline__ void narrow_row(const DevState &s, int sb, float delt
   int changed = 0;
   if (valid && gl == 0) {
     const float nl = updated_label(tw, tl, old, fast);
-    s.vrec[u].lab[sb ^ 1] = nl;
+    dst[u] = nl;
     changed = fabsf(nl - old) > delta;
   }
   changed = __shfl_sync(0xffffffffu, changed, 0, G);
@@ -835,8 +835,8 @@ __device__ __forceinline__ void group_mark(const GV &w, const int (&cand)[32 / G
 
 // One row of any length by a whole warp: 256 slots held as lane + 32*j.
 template <class Mark>
-__device__ __forceinline__ void wide_row(const DevState &s, int sb, float delta, bool fast, int u, int lane,
-                                         Mark mark) {
+__device__ __forceinline__ void wide_row(const DevState &s, const float *src, float *dst, float delta, bool fast,
+                                         int u, int lane, Mark mark) {
   const int2 ri = s.rowinfo[u];
   const int rs = ri.x;
   const int len = ri.y;
@@ -852,7 +852,7 @@ __device__ __forceinline__ void wide_row(const DevState &s, int sb, float delta,
         if (ent.x >= 0) {
           const float wt = __int_as_float(ent.y);
           sw[j] = sw[j] + wt;
-          sl[j] = __fmaf_rn(wt, s.vrec[ent.x].lab[sb], sl[j]);
+          sl[j] = __fmaf_rn(wt, src[ent.x], sl[j]);
         }
       }
     }
@@ -872,9 +872,9 @@ __device__ __forceinline__ void wide_row(const DevState &s, int sb, float delta,
   }
   int changed = 0;
   if (lane == 0) {
-    const float old = s.vrec[u].lab[sb];
+    const float old = src[u];
     const float nl = updated_label(tw, tl, old, fast);
-    s.vrec[u].lab[sb ^ 1] = nl;
+    dst[u] = nl;
     changed = fabsf(nl - old) > delta;
   }
   changed = __shfl_sync(0xffffffffu, changed, 0);
@@ -985,9 +985,8 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
     const unsigned long long prev = atomicCAS(&c.key[h], kEmptyKey, key);
     if (prev == kEmptyKey) {
       const DevState &s = e.recs[g].st;
-      const float2 both = *reinterpret_cast<const float2 *>(s.vrec[v].lab);
-      c.lab[0][h] = both.x;
-      c.lab[1][h] = both.y;
+      c.lab[0][h] = s.lab0[v];
+      c.lab[1][h] = s.lab1[v];
       c.gt[h] = s.gt[v];
       const int len = s.act_len[v];
       c.len[h] = len > kNarrowMax ? kWideLen : static_cast<unsigned char>(len);
@@ -1145,6 +1144,161 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
   }
 }
 
+// Micro mode of the one-block passes: a frontier of at most 32 rows of at
+// most 16 live entries each, all in the row pool, is run by warp 0 alone, one
+// lane per row, with __syncwarp() between passes, while the other warps wait
+// at the block barrier that ends the micro stint. A lane forms its row's two
+// sums in registers: slot t holds entry t, and the reference's tree over 256
+// slots (strides 128..1) adds only +0 at strides 128..16 for such a row, so
+// the tree over 16 slots with strides 8, 4, 2, 1 is exactly the same sum. The
+// marks, the next frontier and its counters are those of the block passes.
+constexpr int kMicroRows = 32;
+constexpr int kMicroLen = 16;
+
+// One micro pass over `cur` (cnt <= 32 rows) with L register slots per lane
+// (every row at most L entries): L = 8 or 16, whichever the warp's longest
+// row needs, so a short row costs half the unrolled work.
+template <int L>
+__device__ __forceinline__ void micro_rows(const EngineArgs &e, SoloCache &c, const unsigned short *cur,
+                                           unsigned short *next, int cnt, int nq, int k, bool rec_any, int su,
+                                           int len) {
+  const int lane = threadIdx.x & 31;
+  const bool valid = lane < cnt;
+  const int off = valid ? c.row[su] : 0;
+  const int src = valid ? (((c.flags[su] >> 2) ^ k) & 1) : 0;
+  float sw[L], sl[L];
+  int col[L];
+#pragma unroll
+  for (int t = 0; t < L; ++t) {
+    sw[t] = 0.0f;
+    sl[t] = 0.0f;
+    col[t] = -1;
+    if (t < len) {
+      const int2 ent = c.rp[off + t];
+      col[t] = ent.x;
+      if (ent.x >= 0) {
+        const float wt = __int_as_float(ent.y);
+        sw[t] = wt;                                       // 0 + w
+        sl[t] = __fmaf_rn(wt, c.lab[src][ent.x], 0.0f);  // fma(w, F_v, 0)
+      }
+    }
+  }
+#pragma unroll
+  for (int h = L / 2; h >= 1; h >>= 1)
+#pragma unroll
+    for (int t = 0; t < h; ++t) {
+      sw[t] = sw[t] + sw[t + h];
+      sl[t] = sl[t] + sl[t + h];
+    }
+  bool changed = false;
+  if (valid) {
+    const int g = c.graph[su];
+    const float old = c.lab[src][su];
+    const float nl = updated_label(sw[0], sl[0], old, e.fast_div);
+    c.lab[src ^ 1][su] = nl;
+    c.flags[su] |= 3;
+    changed = fabsf(nl - old) > e.delta;
+    ++c.visits[su];  // a slot is in a list at most once
+    c.lastpass[g] = k;
+    if (rec_any) {
+      const GraphRec &r = e.recs[g];
+      const int kg = k + r.ba.pass0;
+      if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
+    }
+  }
+  // changed row: its non-deleted, non-GT neighbours and itself
+  // (src/iterativePropagation.cu:200-216)
+  unsigned fresh = 0;  // bit t: entry t newly marked; bit L: the row itself
+  int add = 0, wide = 0;
+  if (changed) {
+#pragma unroll
+    for (int t = 0; t <= L; ++t) {
+      const int ns = t < L ? col[t] : su;
+      if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) {
+        fresh |= 1u << t;
+        const int l = c.len[ns];
+        if (l == kWideLen) wide = 1;
+        else if (c.row[ns] == kNoRow) add += l;
+      }
+    }
+  }
+  const int nf = __popc(fresh);
+  int incl = nf;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int tot = __shfl_sync(0xffffffffu, incl, 31);
+  add = __reduce_add_sync(0xffffffffu, add);
+  wide = __reduce_or_sync(0xffffffffu, wide);
+  int base = 0;
+  if (lane == 0) {  // this warp is the only writer of the counters during the stint
+    base = c.cnt[nq];
+    c.cnt[nq] = base + tot;
+    c.need[nq] += add;
+    if (wide) c.wide[nq] = 1;
+  }
+  int at = __shfl_sync(0xffffffffu, base, 0) + incl - nf;
+#pragma unroll
+  for (int t = 0; t <= L; ++t)
+    if ((fresh >> t) & 1u) next[at++] = static_cast<unsigned short>(t < L ? col[t] : su);
+}
+
+// One micro pass; returns false, having changed nothing, when a row is longer
+// than kMicroLen (the block runs that pass).
+__device__ __forceinline__ bool micro_pass(const EngineArgs &e, SoloCache &c, const unsigned short *cur,
+                                           unsigned short *next, int cnt, int nq, int k, bool rec_any) {
+  const int lane = threadIdx.x & 31;
+  const bool valid = lane < cnt;
+  const int su = valid ? cur[lane] : 0;
+  const int len = valid ? c.len[su] : 0;  // kWideLen for a row longer than 32
+  const int longest = __reduce_max_sync(0xffffffffu, len);
+  if (longest > kMicroLen) return false;
+  if (longest <= 8) micro_rows<8>(e, c, cur, next, cnt, nq, k, rec_any, su, len);
+  else micro_rows<kMicroLen>(e, c, cur, next, cnt, nq, k, rec_any, su, len);
+  return true;
+}
+
+// Runs micro passes from pass k while the frontier qualifies; returns the
+// first pass not run. Called by the 32 threads of warp 0 only.
+__device__ int micro_passes(const EngineArgs &e, SoloCache &c, int k0, int k, int max_iter, bool rec_any,
+                            uint64_t t0) {
+  const int lane = threadIdx.x & 31;
+  const int ng = e.ng;
+  for (;; ++k) {
+    const int j = k - k0;
+    const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
+    const int cnt = c.cnt[q];
+    if (cnt == 0 || cnt > kMicroRows || c.need[q] > 0 || c.wide[q] || k >= max_iter || j >= kSoloMaxPasses ||
+        j >= c.stop_at || (e.pass_budget > 0 && k >= e.pass_budget) || c.used > kVTUse || c.rp_top > kRP)
+      break;
+    if (lane == 0) {
+      const int z = (j + 2) % 3;
+      c.cnt[z] = 0;
+      c.need[z] = 0;
+      c.wide[z] = 0;
+    }
+    if (rec_any)
+      for (int g = lane; g < ng; g += 32) {
+        const GraphRec &r = e.recs[g];
+        const int kg = k + 1 + r.ba.pass0;
+        if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
+      }
+    __syncwarp();
+    if (!micro_pass(e, c, c.list[p], c.list[p ^ 1], cnt, nq, k, rec_any)) break;
+    if (lane == 0 && (j & 15) == 15) {
+      if (global_timer_ns() - t0 > kSoloBudgetNs) c.stop_at = j + 1;
+      if (slice_over(e)) {
+        c.stop_at = j + 1;
+        c.stop_slice = 1;
+      }
+    }
+    __syncwarp();
+  }
+  return k;
+}
+
 // Team mode of the one-block passes: a small frontier whose rows are all in
 // the row pool is run by the block's first kTeamWarps warps, with a named
 // barrier (id 1) of those warps between passes, while the other warps of the
@@ -1261,7 +1415,8 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   __syncthreads();
   const uint64_t t0 = global_timer_ns();
   int k = k0;
-  int team_from = (e.solo & 4) ? k0 : 0x7fffffff;  // team mode is not tried before this pass
+  int team_from = (e.solo & 4) ? k0 : 0x7fffffff;   // team mode is not tried before this pass
+  int micro_from = (e.solo & 8) ? k0 : 0x7fffffff;  // nor micro mode before this one
   for (;; ++k) {
     const int j = k - k0;
     const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
@@ -1272,6 +1427,17 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     if (cnt == 0 || cnt > kSoloList || k >= max_iter || c.wide[q] || j >= kSoloMaxPasses || j >= c.stop_at ||
         (e.pass_budget > 0 && k >= e.pass_budget) || c.used + need > kVTUse || c.rp_top + need > kRP)
       break;
+    if (need == 0 && cnt <= kMicroRows && k >= micro_from) {
+      if (warp == 0) {
+        const int kk = micro_passes(e, c, k0, k, max_iter, rec_any, t0);
+        if (tid == 0) c.team_end = kk;
+      }
+      __syncthreads();  // the other warps wait here for the whole micro stint
+      const int kk = c.team_end;
+      if (kk == k) micro_from = k + 64;  // no pass taken (a row of more than 16): back off
+      k = kk - 1;
+      continue;
+    }
     if (need == 0 && cnt <= kTeamRows && k >= team_from) {
       if (warp < kTeamWarps) {
         const int kk = team_passes(e, c, k0, k, max_iter, rec_any, t0);
@@ -1357,7 +1523,8 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     }
     if (!(c.flags[i] & 1)) continue;
     const int v = static_cast<int>(c.key[i] & 0xffffffffu);
-    *reinterpret_cast<float2 *>(s.vrec[v].lab) = make_float2(c.lab[0][i], c.lab[1][i]);
+    s.lab0[v] = c.lab[0][i];
+    s.lab1[v] = c.lab[1][i];
   }
   // per-graph pass counts, and the frontier back into the set of the graph's
   // pass k + pass0 (the set after it empty)
@@ -1431,13 +1598,15 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     const DevState &s = w.s;
     const int kg = k + w.a.pass0;
     const int nset = (kg + 1) % 3;
-    const int sb = (s.ctl->cur_buf ^ kg) & 1;  // the buffer pass kg reads
+    const int cb = s.ctl->cur_buf;
+    const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
+    float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
     const unsigned stamp = w.g0 + static_cast<unsigned>(kg) + 1u;
     const int u = valid ? s.flist[static_cast<size_t>(kg % 3) * s.n + (item - pref[g])] : 0;
     int len = 0;
     int cand[32 / G + 1];
     unsigned wide_bits = 0;
-    narrow_row<G>(s, sb, w.a.delta, e.fast_div, u, valid, gl, len, cand, wide_bits);
+    narrow_row<G>(s, src, dst, w.a.delta, e.fast_div, u, valid, gl, len, cand, wide_bits);
     group_mark<G>(w, cand, wide_bits, stamp, nset, gl);
     add_keyed(valid && gl == 0, static_cast<unsigned>(len), &s.bc->aff_edges);
     add_keyed(valid && gl == 0, 1u, &s.bc->front_visits);
@@ -1449,7 +1618,9 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     const DevState &s = w.s;
     const int kg = k + w.a.pass0;
     const int nset = (kg + 1) % 3;
-    const int sb = (s.ctl->cur_buf ^ kg) & 1;
+    const int cb = s.ctl->cur_buf;
+    const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
+    float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
     const unsigned stamp = w.g0 + static_cast<unsigned>(kg) + 1u;
     const int u = s.flist[static_cast<size_t>(kg % 3) * s.n + (s.n - 1 - (wi - pref2[g]))];
     auto mark = [&](bool cand, int v) {
@@ -1461,7 +1632,7 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
       }
       frontier_append(w, fresh, first, v, nset);
     };
-    wide_row(s, sb, w.a.delta, e.fast_div, u, lane, mark);
+    wide_row(s, src, dst, w.a.delta, e.fast_div, u, lane, mark);
     if (lane == 0) {
       atomicAdd(&s.bc->aff_edges, static_cast<unsigned long long>(s.act_len[u]));
       atomicAdd(&s.bc->front_visits, 1ull);
@@ -1586,7 +1757,8 @@ __device__ void phase_h(const EngineArgs &e, const Ctx &c, int *pref, int k_end)
       if (i < a.G) {
         const int v = a.gt_ids[i];
         const float l = s.gt[v] == 0 ? 0.0f : 1.0f;
-        *reinterpret_cast<float2 *>(s.vrec[v].lab) = make_float2(l, l);
+        s.lab0[v] = l;
+        s.lab1[v] = l;
       } else if ((i -= a.G) < a.D) {
         s.del_keep[i] = a.del[i];  // the next batch restores these rows (ref)
       } else {
@@ -1601,7 +1773,8 @@ __device__ void phase_h(const EngineArgs &e, const Ctx &c, int *pref, int k_end)
         int now = -1;
         if (st != kDeleted && st != kGroundTruth) {
           const int passes = s.bc->passes;
-          const int pred = s.vrec[v].lab[(s.ctl->cur_buf ^ passes) & 1] >= 0.5f ? 1 : 0;
+          const float *lab = ((s.ctl->cur_buf ^ passes) & 1) ? s.lab1 : s.lab0;
+          const int pred = lab[v] >= 0.5f ? 1 : 0;
           const int truth = s.truth ? s.truth[v] : 0;
           now = pred == truth ? 1 : 0;
         }

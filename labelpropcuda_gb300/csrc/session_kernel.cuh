@@ -61,17 +61,6 @@ struct SessionCtl {
   long long total;
 };
 
-// One 16-byte record per vertex: the two label buffers of the reference's
-// stale double-buffer schedule, and what propagation needs to know about the
-// vertex as a neighbour (bit 0 markable: no ground truth; bit 1 live row
-// longer than 32 entries). A pass reads a neighbour's label and metadata with
-// one load from one 32-byte sector.
-struct alignas(16) VRec {
-  float lab[2];
-  unsigned meta;
-  unsigned pad;
-};
-
 struct DevState {
   int n;
   const int *full_row;      // n+1, full graph
@@ -81,10 +70,12 @@ struct DevState {
   int2 *rowinfo;            // {row start, live row length}: what a propagation pass reads, in one load
   int8_t *status;           // host-side status (src/dynLP.cu:117-130)
   int8_t *gt;               // -1 / 0 / 1
-  VRec *vrec;               // per vertex: both label buffers and the neighbour metadata
+  uint8_t *nmeta;           // what propagation needs about a neighbour, in one byte:
+                            // bit 0 markable (no ground truth), bit 1 live row longer than 32
   const uint8_t *truth;     // 0 / 1
   int *contrib;             // accuracy contribution: -1 none, 0 wrong, 1 right
   const int *batch_map;     // arrival batch per vertex, or null
+  float *lab0, *lab1;
   int *local;               // vertex -> position in this batch's inserted list
   unsigned *del_stamp, *gt_stamp, *dirty_stamp, *front_stamp;
   int *dirty_list;          // n
