@@ -1078,22 +1078,46 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
     // (src/iterativePropagation.cu:200-216). All marks first, then one
     // reservation in the next list for the whole warp.
     unsigned fresh = 0;
-    if (changed) {
+    int add = 0, wide = 0;
+    if constexpr (R <= 8) {
+      // every candidate's class, then every mark, then the marked rows'
+      // lengths: each step's accesses are issued together, not one candidate
+      // at a time
+      int ns[R + 1], gc[R + 1], prev[R + 1], ln[R + 1];
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r) ns[r] = changed ? (r < R ? vv[r] : ((gl == 0 && valid) ? su : -1)) : -1;
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r) gc[r] = ns[r] >= 0 ? c.gt[ns[r]] : 0;
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r) prev[r] = (ns[r] >= 0 && gc[r] < 0) ? atomicMax(&c.mark[ns[r]], k + 1) : k + 1;
 #pragma unroll
       for (int r = 0; r < R + 1; ++r) {
-        const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
-        if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
+        if (prev[r] < k + 1) fresh |= 1u << r;
+        ln[r] = prev[r] < k + 1 ? c.len[ns[r]] : 0;
       }
-    }
-    int add = 0, wide = 0;
 #pragma unroll
-    for (int r = 0; r < R + 1; ++r)
-      if ((fresh >> r) & 1u) {
-        const int ns = r < R ? vv[r] : su;
-        const int l = c.len[ns];
-        if (l == kWideLen) wide = 1;
-        else if (c.row[ns] == kNoRow) add += l;
+      for (int r = 0; r < R + 1; ++r)
+        if ((fresh >> r) & 1u) {
+          if (ln[r] == kWideLen) wide = 1;
+          else if (c.row[ns[r]] == kNoRow) add += ln[r];
+        }
+    } else {
+      if (changed) {
+#pragma unroll
+        for (int r = 0; r < R + 1; ++r) {
+          const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
+          if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
+        }
       }
+#pragma unroll
+      for (int r = 0; r < R + 1; ++r)
+        if ((fresh >> r) & 1u) {
+          const int ns = r < R ? vv[r] : su;
+          const int l = c.len[ns];
+          if (l == kWideLen) wide = 1;
+          else if (c.row[ns] == kNoRow) add += l;
+        }
+    }
     add = __reduce_add_sync(0xffffffffu, add);
     wide = __reduce_or_sync(0xffffffffu, wide);
     if constexpr (R <= 8) {
@@ -1210,7 +1234,28 @@ __device__ __forceinline__ void micro_rows(const EngineArgs &e, SoloCache &c, co
   // (src/iterativePropagation.cu:200-216)
   unsigned fresh = 0;  // bit t: entry t newly marked; bit L: the row itself
   int add = 0, wide = 0;
-  if (changed) {
+  if constexpr (L <= 8) {
+    // every candidate's class, then every mark, then the marked rows'
+    // lengths: each step's accesses are issued together
+    int ns[L + 1], gc[L + 1], prev[L + 1], ln[L + 1];
+#pragma unroll
+    for (int t = 0; t <= L; ++t) ns[t] = changed ? (t < L ? col[t] : su) : -1;
+#pragma unroll
+    for (int t = 0; t <= L; ++t) gc[t] = ns[t] >= 0 ? c.gt[ns[t]] : 0;
+#pragma unroll
+    for (int t = 0; t <= L; ++t) prev[t] = (ns[t] >= 0 && gc[t] < 0) ? atomicMax(&c.mark[ns[t]], k + 1) : k + 1;
+#pragma unroll
+    for (int t = 0; t <= L; ++t) {
+      if (prev[t] < k + 1) fresh |= 1u << t;
+      ln[t] = prev[t] < k + 1 ? c.len[ns[t]] : 0;
+    }
+#pragma unroll
+    for (int t = 0; t <= L; ++t)
+      if ((fresh >> t) & 1u) {
+        if (ln[t] == kWideLen) wide = 1;
+        else if (c.row[ns[t]] == kNoRow) add += ln[t];
+      }
+  } else if (changed) {
 #pragma unroll
     for (int t = 0; t <= L; ++t) {
       const int ns = t < L ? col[t] : su;
