@@ -130,9 +130,7 @@ typedef struct dlp_config {
                               over mid-size frontiers run on a sub-grid with its
                               own barrier; bit 2: within the one-block mode,
                               frontiers of at most 64 loaded rows run on 8 warps
-                              with a named barrier; bit 3: frontiers of at most
-                              32 loaded rows of at most 16 entries run on one
-                              warp, a lane per row. Default 15 (all); same
+                              with a named barrier. Default 7 (all); same
                               results. */
   int solo_entry;        /* one-block mode for total frontiers of at most this
                             many vertices; 0 = 512, at most 1024 (autotuned) */

@@ -117,7 +117,7 @@ class Session:
     def __init__(self, num_nodes: int, row_ptr, col_ind, values, true_labels=None, vertex_batch_map=None, *,
                  tau: float = -1.0, delta: float = 1e-4, max_iterations: int = 100000,
                  semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False, narrow_lanes: int = 0,
-                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: int = 15,
+                 blocks_per_sm: int = 0, wait_timeout_s: float = 2.0, small_frontier_solo: int = 7,
                  solo_entry: int = 0, subgrid_entry: int = 0, arithmetic: int = 0):
         L = _n.lib()
         cfg = _n.Config()
@@ -220,7 +220,7 @@ class Engine:
     def __init__(self, max_graphs: int, memory_budget_bytes: int = 0, *, tau: float = -1.0, delta: float = 1e-4,
                  max_iterations: int = 100000, semantics: int = SEMANTICS_REF, device: int = 0, record: bool = False,
                  narrow_lanes: int = 0, blocks_per_sm: int = 0, wait_timeout_s: float = 2.0,
-                 small_frontier_solo: int = 15, solo_entry: int = 0, subgrid_entry: int = 0,
+                 small_frontier_solo: int = 7, solo_entry: int = 0, subgrid_entry: int = 0,
                  arithmetic: int = 0):
         L = _n.lib()
         cfg = _n.Config()

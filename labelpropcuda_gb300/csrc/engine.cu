@@ -387,7 +387,7 @@ int launch_step(dlp_engine *e, int count, const int *gids, const int *batch_idx,
   args.ng_new = count;
   args.ectl = e->ectl;
   args.timeout_ns = static_cast<unsigned long long>(to * 1e9);
-  args.solo = e->cfg.small_frontier_solo < 0 ? 15 : e->cfg.small_frontier_solo;
+  args.solo = e->cfg.small_frontier_solo < 0 ? 7 : e->cfg.small_frontier_solo;
   args.fast_div = e->cfg.arithmetic == DLP_ARITH_REFERENCE_FAST_MATH ? 1 : 0;
   args.solo_entry = e->cfg.solo_entry > 0 ? e->cfg.solo_entry : dlp::engine::kSoloEntryDefault;
   args.sub_entry = e->cfg.subgrid_entry > 0 ? e->cfg.subgrid_entry : dlp::engine::kSubEntryDefault;
@@ -565,7 +565,7 @@ void dlp_config_default(dlp_config *cfg) {
   cfg->max_iterations = 100000;
   cfg->semantics = DLP_SEMANTICS_REF;
   cfg->wait_timeout_s = 2.0;
-  cfg->small_frontier_solo = 15;
+  cfg->small_frontier_solo = 7;
 }
 
 int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_budget_bytes, dlp_engine **out) {

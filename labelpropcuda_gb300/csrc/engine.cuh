@@ -67,7 +67,7 @@ struct EngineArgs {
   int ng_new;   // the first ng_new of them start a batch; the rest continue one
   EngineCtl *ectl;
   unsigned long long timeout_ns;
-  int solo;  // bit 0: one-block passes; bit 1: sub-grid passes; bit 2: team passes; bit 3: micro passes
+  int solo;  // bit 0: one-block passes; bit 1: sub-grid passes; bit 2: team passes
   int fast_div;    // 1: the reference's fast-math division (dlp_config.arithmetic), else IEEE
   int solo_entry;  // total frontier at most this: one-block passes (<= kSoloEntryMax)
   int sub_entry;   // total frontier at most this: sub-grid passes (<= kSubLive)

@@ -1078,46 +1078,22 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
     // (src/iterativePropagation.cu:200-216). All marks first, then one
     // reservation in the next list for the whole warp.
     unsigned fresh = 0;
-    int add = 0, wide = 0;
-    if constexpr (R <= 8) {
-      // every candidate's class, then every mark, then the marked rows'
-      // lengths: each step's accesses are issued together, not one candidate
-      // at a time
-      int ns[R + 1], gc[R + 1], prev[R + 1], ln[R + 1];
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r) ns[r] = changed ? (r < R ? vv[r] : ((gl == 0 && valid) ? su : -1)) : -1;
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r) gc[r] = ns[r] >= 0 ? c.gt[ns[r]] : 0;
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r) prev[r] = (ns[r] >= 0 && gc[r] < 0) ? atomicMax(&c.mark[ns[r]], k + 1) : k + 1;
+    if (changed) {
 #pragma unroll
       for (int r = 0; r < R + 1; ++r) {
-        if (prev[r] < k + 1) fresh |= 1u << r;
-        ln[r] = prev[r] < k + 1 ? c.len[ns[r]] : 0;
+        const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
+        if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
       }
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r)
-        if ((fresh >> r) & 1u) {
-          if (ln[r] == kWideLen) wide = 1;
-          else if (c.row[ns[r]] == kNoRow) add += ln[r];
-        }
-    } else {
-      if (changed) {
-#pragma unroll
-        for (int r = 0; r < R + 1; ++r) {
-          const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
-          if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r)
-        if ((fresh >> r) & 1u) {
-          const int ns = r < R ? vv[r] : su;
-          const int l = c.len[ns];
-          if (l == kWideLen) wide = 1;
-          else if (c.row[ns] == kNoRow) add += l;
-        }
     }
+    int add = 0, wide = 0;
+#pragma unroll
+    for (int r = 0; r < R + 1; ++r)
+      if ((fresh >> r) & 1u) {
+        const int ns = r < R ? vv[r] : su;
+        const int l = c.len[ns];
+        if (l == kWideLen) wide = 1;
+        else if (c.row[ns] == kNoRow) add += l;
+      }
     add = __reduce_add_sync(0xffffffffu, add);
     wide = __reduce_or_sync(0xffffffffu, wide);
     if constexpr (R <= 8) {
@@ -1166,182 +1142,6 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
         if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
     }
   }
-}
-
-// Micro mode of the one-block passes: a frontier of at most 32 rows of at
-// most 16 live entries each, all in the row pool, is run by warp 0 alone, one
-// lane per row, with __syncwarp() between passes, while the other warps wait
-// at the block barrier that ends the micro stint. A lane forms its row's two
-// sums in registers: slot t holds entry t, and the reference's tree over 256
-// slots (strides 128..1) adds only +0 at strides 128..16 for such a row, so
-// the tree over 16 slots with strides 8, 4, 2, 1 is exactly the same sum. The
-// marks, the next frontier and its counters are those of the block passes.
-constexpr int kMicroRows = 32;
-constexpr int kMicroLen = 16;
-
-// One micro pass over `cur` (cnt <= 32 rows) with L register slots per lane
-// (every row at most L entries): L = 8 or 16, whichever the warp's longest
-// row needs, so a short row costs half the unrolled work.
-template <int L>
-__device__ __forceinline__ void micro_rows(const EngineArgs &e, SoloCache &c, const unsigned short *cur,
-                                           unsigned short *next, int cnt, int nq, int k, bool rec_any, int su,
-                                           int len) {
-  const int lane = threadIdx.x & 31;
-  const bool valid = lane < cnt;
-  const int off = valid ? c.row[su] : 0;
-  const int src = valid ? (((c.flags[su] >> 2) ^ k) & 1) : 0;
-  float sw[L], sl[L];
-  int col[L];
-#pragma unroll
-  for (int t = 0; t < L; ++t) {
-    sw[t] = 0.0f;
-    sl[t] = 0.0f;
-    col[t] = -1;
-    if (t < len) {
-      const int2 ent = c.rp[off + t];
-      col[t] = ent.x;
-      if (ent.x >= 0) {
-        const float wt = __int_as_float(ent.y);
-        sw[t] = wt;                                       // 0 + w
-        sl[t] = __fmaf_rn(wt, c.lab[src][ent.x], 0.0f);  // fma(w, F_v, 0)
-      }
-    }
-  }
-#pragma unroll
-  for (int h = L / 2; h >= 1; h >>= 1)
-#pragma unroll
-    for (int t = 0; t < h; ++t) {
-      sw[t] = sw[t] + sw[t + h];
-      sl[t] = sl[t] + sl[t + h];
-    }
-  bool changed = false;
-  if (valid) {
-    const int g = c.graph[su];
-    const float old = c.lab[src][su];
-    const float nl = updated_label(sw[0], sl[0], old, e.fast_div);
-    c.lab[src ^ 1][su] = nl;
-    c.flags[su] |= 3;
-    changed = fabsf(nl - old) > e.delta;
-    ++c.visits[su];  // a slot is in a list at most once
-    c.lastpass[g] = k;
-    if (rec_any) {
-      const GraphRec &r = e.recs[g];
-      const int kg = k + r.ba.pass0;
-      if (r.ba.record && kg < kRecordIters) atomicAdd(&r.st.rec_fsizes[kg], 1);
-    }
-  }
-  // changed row: its non-deleted, non-GT neighbours and itself
-  // (src/iterativePropagation.cu:200-216)
-  unsigned fresh = 0;  // bit t: entry t newly marked; bit L: the row itself
-  int add = 0, wide = 0;
-  if constexpr (L <= 8) {
-    // every candidate's class, then every mark, then the marked rows'
-    // lengths: each step's accesses are issued together
-    int ns[L + 1], gc[L + 1], prev[L + 1], ln[L + 1];
-#pragma unroll
-    for (int t = 0; t <= L; ++t) ns[t] = changed ? (t < L ? col[t] : su) : -1;
-#pragma unroll
-    for (int t = 0; t <= L; ++t) gc[t] = ns[t] >= 0 ? c.gt[ns[t]] : 0;
-#pragma unroll
-    for (int t = 0; t <= L; ++t) prev[t] = (ns[t] >= 0 && gc[t] < 0) ? atomicMax(&c.mark[ns[t]], k + 1) : k + 1;
-#pragma unroll
-    for (int t = 0; t <= L; ++t) {
-      if (prev[t] < k + 1) fresh |= 1u << t;
-      ln[t] = prev[t] < k + 1 ? c.len[ns[t]] : 0;
-    }
-#pragma unroll
-    for (int t = 0; t <= L; ++t)
-      if ((fresh >> t) & 1u) {
-        if (ln[t] == kWideLen) wide = 1;
-        else if (c.row[ns[t]] == kNoRow) add += ln[t];
-      }
-  } else if (changed) {
-#pragma unroll
-    for (int t = 0; t <= L; ++t) {
-      const int ns = t < L ? col[t] : su;
-      if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) {
-        fresh |= 1u << t;
-        const int l = c.len[ns];
-        if (l == kWideLen) wide = 1;
-        else if (c.row[ns] == kNoRow) add += l;
-      }
-    }
-  }
-  const int nf = __popc(fresh);
-  int incl = nf;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  const int tot = __shfl_sync(0xffffffffu, incl, 31);
-  add = __reduce_add_sync(0xffffffffu, add);
-  wide = __reduce_or_sync(0xffffffffu, wide);
-  int base = 0;
-  if (lane == 0) {  // this warp is the only writer of the counters during the stint
-    base = c.cnt[nq];
-    c.cnt[nq] = base + tot;
-    c.need[nq] += add;
-    if (wide) c.wide[nq] = 1;
-  }
-  int at = __shfl_sync(0xffffffffu, base, 0) + incl - nf;
-#pragma unroll
-  for (int t = 0; t <= L; ++t)
-    if ((fresh >> t) & 1u) next[at++] = static_cast<unsigned short>(t < L ? col[t] : su);
-}
-
-// One micro pass; returns false, having changed nothing, when a row is longer
-// than kMicroLen (the block runs that pass).
-__device__ __forceinline__ bool micro_pass(const EngineArgs &e, SoloCache &c, const unsigned short *cur,
-                                           unsigned short *next, int cnt, int nq, int k, bool rec_any) {
-  const int lane = threadIdx.x & 31;
-  const bool valid = lane < cnt;
-  const int su = valid ? cur[lane] : 0;
-  const int len = valid ? c.len[su] : 0;  // kWideLen for a row longer than 32
-  const int longest = __reduce_max_sync(0xffffffffu, len);
-  if (longest > kMicroLen) return false;
-  if (longest <= 8) micro_rows<8>(e, c, cur, next, cnt, nq, k, rec_any, su, len);
-  else micro_rows<kMicroLen>(e, c, cur, next, cnt, nq, k, rec_any, su, len);
-  return true;
-}
-
-// Runs micro passes from pass k while the frontier qualifies; returns the
-// first pass not run. Called by the 32 threads of warp 0 only.
-__device__ int micro_passes(const EngineArgs &e, SoloCache &c, int k0, int k, int max_iter, bool rec_any,
-                            uint64_t t0) {
-  const int lane = threadIdx.x & 31;
-  const int ng = e.ng;
-  for (;; ++k) {
-    const int j = k - k0;
-    const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
-    const int cnt = c.cnt[q];
-    if (cnt == 0 || cnt > kMicroRows || c.need[q] > 0 || c.wide[q] || k >= max_iter || j >= kSoloMaxPasses ||
-        j >= c.stop_at || (e.pass_budget > 0 && k >= e.pass_budget) || c.used > kVTUse || c.rp_top > kRP)
-      break;
-    if (lane == 0) {
-      const int z = (j + 2) % 3;
-      c.cnt[z] = 0;
-      c.need[z] = 0;
-      c.wide[z] = 0;
-    }
-    if (rec_any)
-      for (int g = lane; g < ng; g += 32) {
-        const GraphRec &r = e.recs[g];
-        const int kg = k + 1 + r.ba.pass0;
-        if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = 0;
-      }
-    __syncwarp();
-    if (!micro_pass(e, c, c.list[p], c.list[p ^ 1], cnt, nq, k, rec_any)) break;
-    if (lane == 0 && (j & 15) == 15) {
-      if (global_timer_ns() - t0 > kSoloBudgetNs) c.stop_at = j + 1;
-      if (slice_over(e)) {
-        c.stop_at = j + 1;
-        c.stop_slice = 1;
-      }
-    }
-    __syncwarp();
-  }
-  return k;
 }
 
 // Team mode of the one-block passes: a small frontier whose rows are all in
@@ -1460,8 +1260,7 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   __syncthreads();
   const uint64_t t0 = global_timer_ns();
   int k = k0;
-  int team_from = (e.solo & 4) ? k0 : 0x7fffffff;   // team mode is not tried before this pass
-  int micro_from = (e.solo & 8) ? k0 : 0x7fffffff;  // nor micro mode before this one
+  int team_from = (e.solo & 4) ? k0 : 0x7fffffff;  // team mode is not tried before this pass
   for (;; ++k) {
     const int j = k - k0;
     const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
@@ -1472,17 +1271,6 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
     if (cnt == 0 || cnt > kSoloList || k >= max_iter || c.wide[q] || j >= kSoloMaxPasses || j >= c.stop_at ||
         (e.pass_budget > 0 && k >= e.pass_budget) || c.used + need > kVTUse || c.rp_top + need > kRP)
       break;
-    if (need == 0 && cnt <= kMicroRows && k >= micro_from) {
-      if (warp == 0) {
-        const int kk = micro_passes(e, c, k0, k, max_iter, rec_any, t0);
-        if (tid == 0) c.team_end = kk;
-      }
-      __syncthreads();  // the other warps wait here for the whole micro stint
-      const int kk = c.team_end;
-      if (kk == k) micro_from = k + 64;  // no pass taken (a row of more than 16): back off
-      k = kk - 1;
-      continue;
-    }
     if (need == 0 && cnt <= kTeamRows && k >= team_from) {
       if (warp < kTeamWarps) {
         const int kk = team_passes(e, c, k0, k, max_iter, rec_any, t0);

@@ -63,8 +63,7 @@ def test_session_matches_oracle(gpu, oracle, cfg):
 
 
 MODES = [
-    dict(),                                            # default: micro, team, one-block, sub-grid, full grid
-    dict(small_frontier_solo=7),                       # without the one-warp micro passes
+    dict(),                                            # default: team, one-block, sub-grid, full grid
     dict(small_frontier_solo=3),                       # one-block passes without the 8-warp team
     dict(small_frontier_solo=1),                       # one-block only
     dict(small_frontier_solo=0),                       # every pass on the full grid
@@ -77,9 +76,9 @@ MODES = [
 @pytest.mark.parametrize("sem", [dlp.SEMANTICS_REF, dlp.SEMANTICS_SPEC])
 @pytest.mark.parametrize("n", [5000, 50000])
 def test_pass_modes_give_identical_results(gpu, sem, n):
-    """The passes give the same results whichever mode runs them: the one-warp
-    micro passes, the 8-warp team, the one-block mode, the sub-grid, the full
-    grid, at any thresholds."""
+    """The passes give the same results whichever mode runs them: the 8-warp
+    team, the one-block mode, the sub-grid, the full grid, at any
+    thresholds."""
     p = dlp.Problem(n, 5, 10, 42)
     runs = [dlp.Session.from_problem(p, semantics=sem, **m) for m in MODES]
     for i, bt in enumerate(p.batches):
