@@ -186,6 +186,18 @@ def algorithmic_bytes(st: dict, num_edges: int, num_inserted: int) -> int:
             + 28 * num_edges + 16 * num_inserted)
 
 
+def mode_delta(before: dict, after: dict, steps: int) -> dict:
+    """Propagation passes and device time per pass mode between two
+    readings, per step, with the time per pass."""
+    out = {}
+    for m, a in after.items():
+        p = a["passes"] - before[m]["passes"]
+        t = a["seconds"] - before[m]["seconds"]
+        out[m] = {"passes": p / max(steps, 1), "ms": 1e3 * t / max(steps, 1),
+                  "us_per_pass": 1e6 * t / p if p else None}
+    return out
+
+
 def percentile(xs, q):
     xs = sorted(xs)
     if not xs:
@@ -368,6 +380,7 @@ def gpu_arm(args, td, rank, world, local_rank):
 
     for _ in range(args.warmup):
         device_step()
+    modes0 = sess.pass_modes()
     sampler = ClockSampler(local_rank)
     sampler.start()
     dist_barrier(td)
@@ -381,6 +394,7 @@ def gpu_arm(args, td, rank, world, local_rank):
         edges += sum(s["affected_edges"] for s in stats)
     dist_barrier(td)
     clocks = sampler.stop()
+    modes = mode_delta(modes0, sess.pass_modes(), args.steps)
     t_dev = sum(step_ms) / 1e3
     t_max = dist_max(td, t_dev)
     edges_all = dist_sum(td, edges)
@@ -467,6 +481,7 @@ def gpu_arm(args, td, rank, world, local_rank):
         "fp64_oracle_error": fp64,
         "reference_cuda": ref_cuda,
         "clocks": clocks,
+        "pass_modes_per_step": modes,
         "gpu_launches": args.steps * nb * 2,
     }
     if args.per_batch:
@@ -626,19 +641,20 @@ def served_block(args, local_rank, rank=0, world=1, td=None) -> dict:
     # batched: one launch per step over every graph
     def batched_run():
         reset_all()
+        m0 = eng.pass_modes()
         first = eng.steps
         for b in range(nb):
             eng.step_device([(g, skip + b, packed[b].view(i)) for i, g in enumerate(gids)])
         eng.synchronize()
         ms = [eng.elapsed_ms(first + b, first + b) for b in range(nb)]
         ae = sum(eng.stats(g, skip + b)["affected_edges"] for g in gids for b in range(nb))
-        return ms, ae
-    b_ms, b_ae = batched_run()
+        return ms, ae, mode_delta(m0, eng.pass_modes(), 1)
+    b_ms, b_ae, b_modes = batched_run()
     b_t = dist_max(td, sum(b_ms) / 1e3)
     b_ae = int(dist_sum(td, b_ae))
     batched = {"value": b_ae / b_t, "ms_per_step": 1e3 * b_t / nb,
                "step_ms_p50": percentile(b_ms, 0.5), "step_ms_max": max(b_ms),
-               "affected_edges": b_ae, "launches": 2 * nb,
+               "affected_edges": b_ae, "launches": 2 * nb, "pass_modes": b_modes,
                "timing": "CUDA events around each step, batches resident in HBM"}
     progress(f"batched {batched['value'] / 1e9:.3f} G/s, step max {max(b_ms):.0f} ms")
 

@@ -283,6 +283,12 @@ int dlp_engine_steps(const dlp_engine *e);
  * of the last one-block / sub-grid stint. */
 int dlp_engine_debug(dlp_engine *e, int *out4);
 int dlp_engine_elapsed_ms(dlp_engine *e, int first_step, int last_step, float *ms);
+/* Propagation passes the engine's launches have run so far, by mode, and the
+ * device time they took: [0] one block (including [1]), [1] the 8-warp team,
+ * [2] the 16-block sub-grid, [3] the full grid. Diagnostics of where a
+ * workload's propagation time goes; cumulative since the engine was made. */
+int dlp_engine_pass_modes(dlp_engine *e, unsigned long long *passes4, double *seconds4);
+int dlp_session_pass_modes(dlp_session *s, unsigned long long *passes4, double *seconds4);
 int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels);
 int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, int64_t capacity,
                         int64_t *count);

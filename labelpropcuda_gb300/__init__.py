@@ -193,6 +193,14 @@ class Session:
         _n.check(_n.lib().dlp_session_elapsed_ms(self._h, first, last, ctypes.byref(ms)))
         return float(ms.value)
 
+    def pass_modes(self) -> dict:
+        """Propagation passes so far by mode and their device seconds."""
+        p = (ctypes.c_ulonglong * 4)()
+        t = (ctypes.c_double * 4)()
+        _n.check(_n.lib().dlp_session_pass_modes(self._h, p, t))
+        names = ("one_block", "team", "sub_grid", "full_grid")
+        return {n: {"passes": int(p[i]), "seconds": float(t[i])} for i, n in enumerate(names)}
+
     def debug(self) -> dict:
         out = (ctypes.c_int * 4)()
         _n.check(_n.lib().dlp_session_debug(self._h, out))
@@ -349,6 +357,14 @@ class Engine:
     @property
     def steps(self) -> int:
         return int(_n.lib().dlp_engine_steps(self._h))
+
+    def pass_modes(self) -> dict:
+        """Propagation passes so far by mode and their device seconds."""
+        p = (ctypes.c_ulonglong * 4)()
+        t = (ctypes.c_double * 4)()
+        _n.check(_n.lib().dlp_engine_pass_modes(self._h, p, t))
+        names = ("one_block", "team", "sub_grid", "full_grid")
+        return {n: {"passes": int(p[i]), "seconds": float(t[i])} for i, n in enumerate(names)}
 
     def elapsed_ms(self, first_step: int, last_step: int) -> float:
         ms = ctypes.c_float(0.0)

@@ -169,6 +169,8 @@ _SIGNATURES = {
     "dlp_engine_restore_as": (_I, [_P, _P, ctypes.c_size_t, _I]),
     "dlp_engine_graph_resident_bytes": (ctypes.c_size_t, [_P, _I]),
     "dlp_engine_hold_id": (_I, [_P, _I]),
+    "dlp_engine_pass_modes": (_I, [_P, _P, _P]),
+    "dlp_session_pass_modes": (_I, [_P, _P, _P]),
     "dlp_engine_release_id": (_I, [_P, _I]),
     "dlp_server_evictions": (_I, [_P, c_int_p, c_int_p]),
     "dlp_server_make_resident": (_I, [_P, _I]),

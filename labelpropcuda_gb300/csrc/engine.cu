@@ -1063,6 +1063,20 @@ int dlp_engine_debug(dlp_engine *e, int *out4) {
   return DLP_OK;
 }
 
+int dlp_engine_pass_modes(dlp_engine *e, unsigned long long *passes4, double *seconds4) {
+  dlp::clear_error();
+  if (!e || !passes4 || !seconds4) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+  DLP_CUDA_TRY(cudaSetDevice(e->device));
+  DLP_CUDA_TRY(cudaStreamSynchronize(e->stream));
+  EngineCtl c;
+  DLP_CUDA_TRY(cudaMemcpy(&c, e->ectl, sizeof(c), cudaMemcpyDeviceToHost));
+  for (int m = 0; m < 4; ++m) {
+    passes4[m] = c.mode_passes[m];
+    seconds4[m] = static_cast<double>(c.mode_ns[m]) * 1e-9;
+  }
+  return DLP_OK;
+}
+
 int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels) {
   dlp::clear_error();
   GraphSlot *g = slot_of(e, graph_id);
@@ -1215,6 +1229,12 @@ int dlp_session_elapsed_ms(dlp_session *s, int first, int last, float *ms) {
 int dlp_session_read_labels(dlp_session *s, float *host_labels) {
   if (!s) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null session");
   return dlp_engine_read_labels(s->eng, s->gid, host_labels);
+}
+
+int dlp_session_pass_modes(dlp_session *s, unsigned long long *passes4, double *seconds4) {
+  dlp::clear_error();
+  if (!s) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null session");
+  return dlp_engine_pass_modes(s->eng, passes4, seconds4);
 }
 
 int dlp_session_debug(dlp_session *s, int *out4) {

@@ -59,6 +59,11 @@ struct EngineCtl {
   int where_pass;       // last propagation pass block 0 started
   unsigned long long slice_stop;  // the launch's time slice ran out
   unsigned long long t_launch;  // global timer at the start of the launch (thread 0 of block 0)
+  // Propagation passes run so far by mode, and the device time they took
+  // (global timer): 0 one block, 1 of which the 8-warp team, 2 sub-grid,
+  // 3 full grid. Written by thread 0 of block 0 only, once per launch.
+  unsigned long long mode_passes[4];
+  unsigned long long mode_ns[4];
 };
 
 struct EngineArgs {

@@ -1261,6 +1261,7 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   const uint64_t t0 = global_timer_ns();
   int k = k0;
   int team_from = (e.solo & 4) ? k0 : 0x7fffffff;  // team mode is not tried before this pass
+  unsigned long long team_count = 0, team_ns = 0;   // thread 0: team passes of this stint, their time
   for (;; ++k) {
     const int j = k - k0;
     const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
@@ -1272,12 +1273,17 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
         (e.pass_budget > 0 && k >= e.pass_budget) || c.used + need > kVTUse || c.rp_top + need > kRP)
       break;
     if (need == 0 && cnt <= kTeamRows && k >= team_from) {
+      const uint64_t tt = tid == 0 ? global_timer_ns() : 0;
       if (warp < kTeamWarps) {
         const int kk = team_passes(e, c, k0, k, max_iter, rec_any, t0);
         if (tid == 0) c.team_end = kk;
       }
       __syncthreads();  // the other warps wait here for the whole team stint
       const int kk = c.team_end;
+      if (tid == 0) {
+        team_count += kk - k;
+        team_ns += global_timer_ns() - tt;
+      }
       if (kk == k) team_from = k + 1;  // no pass taken: the block runs this one
       k = kk - 1;  // the loop increment resumes at pass kk
       continue;
@@ -1398,6 +1404,8 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   if (tid == 0) {
     e.ectl->solo_k[slot] = k;
     e.ectl->solo_passes[slot] = k - k0;
+    e.ectl->mode_passes[1] += team_count;
+    e.ectl->mode_ns[1] += team_ns;
   }
 }
 
@@ -1530,6 +1538,8 @@ __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2
   int solo_from = 0;     // the one-block mode declined: not tried again before this pass
   int stint = 0;
   int k = 0;
+  // thread 0 of block 0: passes and device time per mode in this launch
+  unsigned long long mp[3] = {0, 0, 0}, mns[3] = {0, 0, 0};  // one block, sub-grid, full grid
   for (;; ++k) {
     int tn, tw;
     pass_sizes(e, k, pref, pref2, tn, tw);
@@ -1541,6 +1551,7 @@ __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2
     const bool sub_ok = !solo_ok && (e.solo & 2) && gridDim.x > 2 * kSubBlocks && tn + tw <= e.sub_entry &&
                         k != no_small_at;
     if (solo_ok || sub_ok) {
+      const uint64_t ts = c.gtid == 0 ? global_timer_ns() : 0;
       if (solo_ok) {
         if (blockIdx.x == 0) solo_passes<kSoloG>(e, k, stint & 1, solo);
       } else if (blockIdx.x < kSubBlocks) {
@@ -1550,16 +1561,33 @@ __device__ bool phase_g(const EngineArgs &e, const Ctx &c, int *pref, int *pref2
       const int done = ld_relaxed_i32(&e.ectl->solo_passes[stint & 1]);
       const int kk = ld_relaxed_i32(&e.ectl->solo_k[stint & 1]);
       ++stint;
+      if (c.gtid == 0) {
+        mp[solo_ok ? 0 : 1] += done;
+        mns[solo_ok ? 0 : 1] += global_timer_ns() - ts;
+      }
       if (done == 0) no_small_at = k;
       if (solo_ok && done == 0) solo_from = k + 256;
       k = kk - 1;  // the loop increment resumes at pass kk
       continue;
     }
+    const uint64_t tp = c.gtid == 0 ? global_timer_ns() : 0;
     run_pass<G>(e, k, pref, tn, pref2, tw, c.lane, c.gwarp, c.nwarps, c.gtid, c.nthreads);
     if (c.gtid == 0 && slice_over(e)) e.ectl->slice_stop = stop_code(e, k + 1);
     if (!grid_sync(&e.ectl->bar, &e.ectl->err, e.timeout_ns)) return false;
+    if (c.gtid == 0) {
+      ++mp[2];
+      mns[2] += global_timer_ns() - tp;
+    }
   }
   k_end = k;
+  if (c.gtid == 0) {
+    e.ectl->mode_passes[0] += mp[0];
+    e.ectl->mode_ns[0] += mns[0];
+    e.ectl->mode_passes[2] += mp[1];
+    e.ectl->mode_ns[2] += mns[1];
+    e.ectl->mode_passes[3] += mp[2];
+    e.ectl->mode_ns[3] += mns[2];
+  }
   return true;
 }
 
