@@ -112,6 +112,10 @@ bool runDynLP(const DynLPConfig &config, const CSRGraph &graph, const std::vecto
   cfg.tau = config.tau;
   cfg.delta = config.delta;
   cfg.max_iterations = config.maxIterations;
+  // DynLPConfig has no field for it: DLP_ARITHMETIC=reference_fast_math in the
+  // environment selects the reference's fast-math division for this run
+  if (const char *a = std::getenv("DLP_ARITHMETIC"))
+    if (std::string(a) == "reference_fast_math") cfg.arithmetic = DLP_ARITH_REFERENCE_FAST_MATH;
   int dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess) cfg.device = dev;
 
