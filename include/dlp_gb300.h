@@ -284,9 +284,10 @@ int dlp_engine_steps(const dlp_engine *e);
 int dlp_engine_debug(dlp_engine *e, int *out4);
 int dlp_engine_elapsed_ms(dlp_engine *e, int first_step, int last_step, float *ms);
 /* Propagation passes the engine's launches have run so far, by mode, and the
- * device time they took: [0] one block (including [1]), [1] the 8-warp team,
- * [2] the 16-block sub-grid, [3] the full grid. Diagnostics of where a
- * workload's propagation time goes; cumulative since the engine was made. */
+ * device time they took: [0] one block (including [1]), [1] the 8-warp team
+ * (passes only; its time is counted in [0]), [2] the 16-block sub-grid,
+ * [3] the full grid. Diagnostics of where a workload's propagation time goes;
+ * cumulative since the engine was made. */
 int dlp_engine_pass_modes(dlp_engine *e, unsigned long long *passes4, double *seconds4);
 int dlp_session_pass_modes(dlp_session *s, unsigned long long *passes4, double *seconds4);
 int dlp_engine_read_labels(dlp_engine *e, int graph_id, float *host_labels);

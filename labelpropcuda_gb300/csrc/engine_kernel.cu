@@ -1261,7 +1261,7 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   const uint64_t t0 = global_timer_ns();
   int k = k0;
   int team_from = (e.solo & 4) ? k0 : 0x7fffffff;  // team mode is not tried before this pass
-  unsigned long long team_count = 0, team_ns = 0;   // thread 0: team passes of this stint, their time
+  unsigned long long team_count = 0;  // thread 0: team passes of this stint
   for (;; ++k) {
     const int j = k - k0;
     const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
@@ -1273,17 +1273,13 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
         (e.pass_budget > 0 && k >= e.pass_budget) || c.used + need > kVTUse || c.rp_top + need > kRP)
       break;
     if (need == 0 && cnt <= kTeamRows && k >= team_from) {
-      const uint64_t tt = tid == 0 ? global_timer_ns() : 0;
       if (warp < kTeamWarps) {
         const int kk = team_passes(e, c, k0, k, max_iter, rec_any, t0);
         if (tid == 0) c.team_end = kk;
       }
       __syncthreads();  // the other warps wait here for the whole team stint
       const int kk = c.team_end;
-      if (tid == 0) {
-        team_count += kk - k;
-        team_ns += global_timer_ns() - tt;
-      }
+      if (tid == 0) team_count += kk - k;
       if (kk == k) team_from = k + 1;  // no pass taken: the block runs this one
       k = kk - 1;  // the loop increment resumes at pass kk
       continue;
@@ -1404,8 +1400,7 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   if (tid == 0) {
     e.ectl->solo_k[slot] = k;
     e.ectl->solo_passes[slot] = k - k0;
-    e.ectl->mode_passes[1] += team_count;
-    e.ectl->mode_ns[1] += team_ns;
+    e.ectl->mode_passes[1] += team_count;  // their time is part of the one-block stint's
   }
 }
 
