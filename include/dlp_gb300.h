@@ -121,8 +121,11 @@ typedef struct dlp_config {
   int semantics;         /* enum dlp_semantics */
   int device;            /* CUDA device ordinal */
   int record;            /* nonzero: keep per-batch artefacts for dlp_session_artefact */
-  int narrow_lanes;      /* lanes per short row in propagation: 4, 8, 16 or 32; 0 = 8
-                            (dlp_autotune picks one for a workload) */
+  int narrow_lanes;      /* lanes per short row in full-grid propagation passes: 4, 8,
+                            16 or 32; or 1: one lane per row of at most 8 entries
+                            (32 rows in flight per warp) and 4-lane groups for rows
+                            of 9 to 32; 0 = 8 (dlp_autotune picks one for a
+                            workload); same results */
   int blocks_per_sm;     /* persistent grid occupancy; 0 = from the occupancy query */
   double wait_timeout_s; /* limit for any device-side wait; <= 0: 2 s */
   int small_frontier_solo; /* bit 0: passes over small frontiers run on one
@@ -300,7 +303,7 @@ int dlp_engine_artefact(dlp_engine *e, int graph_id, int which, void *host_out, 
  * block, a 16-block sub-grid or the whole grid by the size of the frontier.
  * The lane width of the short-row bucket, the two frontier thresholds
  * (solo_entry, subgrid_entry) and the persistent grid's blocks per SM are
- * chosen by timing every candidate (lanes 4/8/16 x one-block entry
+ * chosen by timing every candidate (lanes 1/4/8 x one-block entry
  * 256/512/1024 x sub-grid entry 1024/2048/4096 x the blocks per SM the build
  * allows) on a sample the library generates with the reference generator:
  * num_graphs graphs of sizes[i] vertices and average degree degrees[i],

@@ -579,8 +579,8 @@ int dlp_engine_create(const dlp_config *cfg_in, int max_graphs, size_t memory_bu
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "max_graphs must be in [1, 1024]");
   if (!(cfg.delta > 0.0f)) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "delta must be positive");
   const int lanes = cfg.narrow_lanes == 0 ? 8 : cfg.narrow_lanes;
-  if (lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
-    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "narrow_lanes must be 4, 8, 16 or 32");
+  if (lanes != 1 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "narrow_lanes must be 1, 4, 8, 16 or 32");
   if (cfg.arithmetic != DLP_ARITH_IEEE && cfg.arithmetic != DLP_ARITH_REFERENCE_FAST_MATH)
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "arithmetic must be DLP_ARITH_IEEE or DLP_ARITH_REFERENCE_FAST_MATH");
   if (cfg.solo_entry < 0 || cfg.solo_entry > dlp::engine::kSoloEntryMax || cfg.subgrid_entry < 0 ||

@@ -1404,6 +1404,112 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   }
 }
 
+// One row of at most kLaneRow live entries by one lane, its 8-slot tree in
+// registers (slot t = entry t). For such a row the reference's tree over 256
+// slots adds only +0 at strides 128..8, so strides 4, 2, 1 give exactly its
+// sum — the same as narrow_row<G>. cand[] and wide_bits as in narrow_row.
+constexpr int kLaneRow = 8;
+
+__device__ __forceinline__ void lane_row(const DevState &s, const float *src, float *dst, float delta, bool fast,
+                                         int u, int rs, int len, bool valid, int (&cand)[kLaneRow + 1],
+                                         unsigned &wide_bits) {
+  float sw[kLaneRow], sl[kLaneRow];
+  int vv[kLaneRow];
+  unsigned wb = 0;
+  const float old = valid ? src[u] : 0.0f;
+#pragma unroll
+  for (int t = 0; t < kLaneRow; ++t) {
+    sw[t] = 0.0f;
+    sl[t] = 0.0f;
+    vv[t] = -1;
+    if (valid && t < len) {
+      const int2 ent = s.act_adj[rs + t];
+      if (ent.x >= 0) {
+        const float wt = __int_as_float(ent.y);
+        sw[t] = wt;                               // 0 + w
+        sl[t] = __fmaf_rn(wt, src[ent.x], 0.0f);  // fma(w, F_v, 0)
+        const unsigned meta = s.nmeta[ent.x];
+        if (meta & 1u) vv[t] = ent.x;
+        if (meta & 2u) wb |= 1u << t;
+      }
+    }
+  }
+#pragma unroll
+  for (int h = kLaneRow / 2; h >= 1; h >>= 1)
+#pragma unroll
+    for (int t = 0; t < h; ++t) {
+      sw[t] = sw[t] + sw[t + h];
+      sl[t] = sl[t] + sl[t + h];
+    }
+  bool changed = false;
+  if (valid) {
+    const float nl = updated_label(sw[0], sl[0], old, fast);
+    dst[u] = nl;
+    changed = fabsf(nl - old) > delta;
+  }
+#pragma unroll
+  for (int t = 0; t < kLaneRow; ++t) cand[t] = changed ? vv[t] : -1;
+  cand[kLaneRow] = changed ? u : -1;
+  wide_bits = changed ? wb : 0u;
+}
+
+// Marks of one-lane rows: every stamp atomic is issued before any result is
+// used; then the lanes of one graph (a contiguous run: the work list is
+// sorted by graph, invalid lanes last) reserve their next-frontier and
+// touched-list entries with one atomic per list per run.
+__device__ __forceinline__ void lane_mark(const GV &w, bool valid, int key, const int (&cand)[kLaneRow + 1],
+                                          unsigned wide_bits, unsigned stamp, int set, int lane) {
+  constexpr int C = kLaneRow + 1;
+  const DevState &s = w.s;
+  unsigned old[C];
+#pragma unroll
+  for (int r = 0; r < C; ++r) old[r] = cand[r] >= 0 ? atomicMax(&s.front_stamp[cand[r]], stamp) : stamp;
+  int nn = 0, nw = 0, nf = 0;
+#pragma unroll
+  for (int r = 0; r < C; ++r) {
+    if (old[r] < stamp) {
+      if ((wide_bits >> r) & 1u) ++nw;
+      else ++nn;
+    }
+    if (old[r] < w.g0) ++nf;
+  }
+  // counts packed 10 bits each (a run of 32 lanes marks at most 288)
+  const int mine = nn | (nw << 10) | (nf << 20);
+  int incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    const int kp = __shfl_up_sync(0xffffffffu, key, o);
+    if (lane >= o && kp == key) incl += t;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  const int tail = 31 - __clz(peers);
+  const int tot = __shfl_sync(0xffffffffu, incl, tail);
+  int bn = 0, bw = 0, bf = 0;
+  if (lane == tail && valid && tot != 0) {
+    const int tn = tot & 1023, tw = (tot >> 10) & 1023, tf = tot >> 20;
+    if (tn) bn = atomicAdd(&s.bc->front_count[set][0], tn);
+    if (tw) bw = atomicAdd(&s.bc->front_count[set][1], tw);
+    if (tf) bf = atomicAdd(&s.ctl->touched_count[w.a.seq & 1], tf);
+  }
+  bn = __shfl_sync(0xffffffffu, bn, tail);
+  bw = __shfl_sync(0xffffffffu, bw, tail);
+  bf = __shfl_sync(0xffffffffu, bf, tail);
+  if (!valid || mine == 0) return;
+  const int excl = incl - mine;
+  int on = bn + (excl & 1023), ow = bw + ((excl >> 10) & 1023), of = bf + (excl >> 20);
+  int *list = s.flist + static_cast<size_t>(set) * s.n;
+  int *touched = s.touched + static_cast<size_t>(w.a.seq & 1) * s.n;
+#pragma unroll
+  for (int r = 0; r < C; ++r) {
+    if (old[r] < stamp) {
+      if ((wide_bits >> r) & 1u) list[s.n - 1 - ow++] = cand[r];
+      else list[on++] = cand[r];
+    }
+    if (old[r] < w.g0) touched[of++] = cand[r];
+  }
+}
+
 // One propagation pass k over the flattened frontier, by the warps
 // [warp0, warp0 + nwarps) and threads [t0, t0 + nthreads) of the launch.
 template <int G>
@@ -1425,6 +1531,63 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
       if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = nn + nw;
     }
   }
+  if constexpr (G == 1) {
+    // rows of at most 32 entries: one lane per row of at most 8 entries, 32
+    // rows in flight per warp; rows of 9 to 32 entries of the same 32 go to
+    // 4-lane groups afterwards
+    for (int base = warp0 * 32; base < tn; base += nwarps * 32) {
+      const int item = base + lane;
+      const bool valid = item < tn;
+      const int g = valid ? locate(pref, ng, item) : 0;
+      int u = 0, rs = 0, len = 0;
+      {
+        const GV w = view(e, g);
+        const DevState &s = w.s;
+        const int kg = k + w.a.pass0;
+        const int cb = s.ctl->cur_buf;
+        const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
+        float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
+        if (valid) {
+          u = s.flist[static_cast<size_t>(kg % 3) * s.n + (item - pref[g])];
+          const int2 ri = s.rowinfo[u];
+          rs = ri.x;
+          len = ri.y;
+        }
+        const bool mine = valid && len <= kLaneRow;
+        int cand[kLaneRow + 1];
+        unsigned wide_bits = 0;
+        lane_row(s, src, dst, w.a.delta, e.fast_div, u, rs, len, mine, cand, wide_bits);
+        lane_mark(w, mine, valid ? g : -1, cand, wide_bits, w.g0 + static_cast<unsigned>(kg) + 1u, (kg + 1) % 3,
+                  lane);
+        add_keyed(mine, static_cast<unsigned>(len), &s.bc->aff_edges);
+        add_keyed(mine, 1u, &s.bc->front_visits);
+      }
+      unsigned longm = __ballot_sync(0xffffffffu, valid && len > kLaneRow);
+      const int q = lane >> 2, ql = lane & 3;
+      while (longm) {  // up to 8 rows a round, the q-th remaining one to 4-lane group q
+        unsigned m = longm;
+        for (int i = 0; i < q && m; ++i) m &= m - 1;
+        const bool have = m != 0;
+        const int from = have ? __ffs(m) - 1 : 0;
+        const int gq = __shfl_sync(0xffffffffu, g, from);
+        const int uq = __shfl_sync(0xffffffffu, u, from);
+        for (int i = 0; i < 8 && longm; ++i) longm &= longm - 1;
+        const GV w = view(e, gq);
+        const DevState &s = w.s;
+        const int kg = k + w.a.pass0;
+        const int cb = s.ctl->cur_buf;
+        const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
+        float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
+        int lq = 0;
+        int cand[32 / 4 + 1];
+        unsigned wide_bits = 0;
+        narrow_row<4>(s, src, dst, w.a.delta, e.fast_div, uq, have, ql, lq, cand, wide_bits);
+        group_mark<4>(w, cand, wide_bits, w.g0 + static_cast<unsigned>(kg) + 1u, (kg + 1) % 3, ql);
+        add_keyed(have && ql == 0, static_cast<unsigned>(lq), &s.bc->aff_edges);
+        add_keyed(have && ql == 0, 1u, &s.bc->front_visits);
+      }
+    }
+  } else
   // rows of at most 32 entries: groups of G lanes
   for (int base = warp0 * GPW; base < tn; base += nwarps * GPW) {
     const int item = base + grp;
@@ -1476,16 +1639,61 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
   }
 }
 
-// Frontier sizes of pass k: narrow rows into pref, wide rows into pref2.
+// Frontier sizes of pass k: narrow rows into pref, wide rows into pref2. Both
+// prefixes come from one scan: a graph's two counts are read once and summed
+// as the halves of one 64-bit value (a frontier never reaches 2^32 rows).
 __device__ __forceinline__ void pass_sizes(const EngineArgs &e, int k, int *pref, int *pref2, int &tn, int &tw) {
-  tn = flat_build(pref, e.ng, [&](int g) {
-    int nn, nw;
-    return graph_in_pass(e.recs[g], k, nn, nw) ? nn : 0;
-  });
-  tw = flat_build(pref2, e.ng, [&](int g) {
-    int nn, nw;
-    return graph_in_pass(e.recs[g], k, nn, nw) ? nw : 0;
-  });
+  __shared__ unsigned long long s_warp2[kBlock / 32];
+  const int ng = e.ng;
+  __syncthreads();
+  constexpr int kPer = (kMaxGraphs + kBlock - 1) / kBlock;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long vals[kPer];
+  unsigned long long local = 0;
+  const int start = threadIdx.x * kPer;
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int g = start + j;
+    int nn = 0, nw = 0;
+    if (g < ng && !graph_in_pass(e.recs[g], k, nn, nw)) nn = nw = 0;
+    vals[j] = (static_cast<unsigned long long>(nw) << 32) | static_cast<unsigned>(nn);
+    local += vals[j];
+  }
+  unsigned long long incl = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp2[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long x = lane < kBlock / 32 ? s_warp2[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane < kBlock / 32) s_warp2[lane] = x;
+  }
+  __syncthreads();
+  unsigned long long run = incl - local + (warp > 0 ? s_warp2[warp - 1] : 0);
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int g = start + j;
+    if (g < ng) {
+      pref[g] = static_cast<int>(run & 0xffffffffu);
+      pref2[g] = static_cast<int>(run >> 32);
+    }
+    run += vals[j];
+  }
+  if (threadIdx.x == kBlock - 1) {
+    pref[ng] = static_cast<int>(run & 0xffffffffu);
+    pref2[ng] = static_cast<int>(run >> 32);
+  }
+  __syncthreads();
+  tn = pref[ng];
+  tw = pref2[ng];
 }
 
 // Sub-grid mode: mid-size frontiers are run by the first kSubBlocks blocks
@@ -1751,6 +1959,7 @@ __global__ void __launch_bounds__(kBlock, 1024 / kBlock) engine_kernel(EngineArg
   }
 }
 
+template __global__ void engine_kernel<1>(EngineArgs);
 template __global__ void engine_kernel<4>(EngineArgs);
 template __global__ void engine_kernel<8>(EngineArgs);
 template __global__ void engine_kernel<16>(EngineArgs);
@@ -1771,6 +1980,7 @@ size_t engine_dynamic_smem() { return sizeof(SoloCache); }
 
 const void *engine_kernel_ptr(int lanes) {
   switch (lanes) {
+    case 1: return reinterpret_cast<const void *>(&engine_kernel<1>);
     case 4: return reinterpret_cast<const void *>(&engine_kernel<4>);
     case 8: return reinterpret_cast<const void *>(&engine_kernel<8>);
     case 16: return reinterpret_cast<const void *>(&engine_kernel<16>);

@@ -3,8 +3,8 @@
 // fixed (256-thread blocks, one block per row, src/iterativePropagation.cu).
 //
 // The engine's propagation splits rows into two degree buckets: rows of at
-// most 32 live entries go to groups of `narrow_lanes` lanes (4, 8, 16 or 32),
-// longer rows to whole warps. Each pass also picks its launch mode by the
+// most 32 live entries go to groups of `narrow_lanes` lanes (4, 8, 16 or 32;
+// or 1: a lane per row of at most 8 entries), longer rows to whole warps. Each pass also picks its launch mode by the
 // total frontier: one block (up to solo_entry vertices), a 16-block sub-grid
 // (up to subgrid_entry) or the whole grid. The tunables are the lane width of
 // the short-row bucket, the two frontier thresholds and the persistent grid's
@@ -113,7 +113,7 @@ int dlp_autotune(dlp_config *cfg, int num_graphs, const int *sizes, const int *d
     }
     bmaps.push_back(std::move(m));
   }
-  static const int kLanes[] = {4, 8, 16};
+  static const int kLanes[] = {1, 4, 8};
   static const int kSoloEntries[] = {256, 512, 1024};
   static const int kSubEntries[] = {1024, 2048, 4096};
   // blocks per SM the build's block size allows (1024-thread blocks: one)

@@ -106,8 +106,9 @@ def test_multi_instance_sample_matches_oracle(gpu, oracle):
     """16 graphs of the 512-graph multi-instance set (n log-uniform on
     [1e3, 5e5], degree {3,5,7}, seeds i): the smallest, the largest and 14
     evenly spaced by size between them, all stepped together in one launch per
-    step for all 10 batches, each checked against its own oracle run. A
-    second engine runs every pass on the full grid with 4-lane groups.
+    step for all 10 batches, each checked against its own oracle run. Two
+    more engines run every pass on the full grid, with 4-lane groups and with
+    a lane per short row.
     Propagation is capped at 1,000 passes per batch on both sides (the
     workload's 100,000 would keep the oracle busy for many minutes on the
     batches that never converge); everything else is the workload's."""
@@ -119,7 +120,8 @@ def test_multi_instance_sample_matches_oracle(gpu, oracle):
     cap = 1000
     orcs = [oracle.OracleRun.from_problem(p, threads=0, max_iterations=cap) for p in probs]
     engines = [dlp.Engine(len(probs), max_iterations=cap),
-               dlp.Engine(len(probs), max_iterations=cap, small_frontier_solo=0, narrow_lanes=4)]
+               dlp.Engine(len(probs), max_iterations=cap, small_frontier_solo=0, narrow_lanes=4),
+               dlp.Engine(len(probs), max_iterations=cap, small_frontier_solo=0, narrow_lanes=1)]
     gids = [[e.add_problem(p) for p in probs] for e in engines]
     for b in range(10):
         want = [(o.apply(b, p.batches[b]), o.labels()) for o, p in zip(orcs, probs)]

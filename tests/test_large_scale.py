@@ -62,14 +62,15 @@ ORACLE_BATCHES = 6
 @pytest.mark.gpu
 def test_largest_configuration_first_batches_match_oracle(gpu, oracle):
     """The first batches of the 20,000,000-vertex problem against the oracle
-    (all host threads), element by element, in two launch shapes: the default
-    (small frontiers on one block or a 16-block sub-grid) and every pass on
-    the full grid with 4-lane row groups."""
+    (all host threads), element by element, in three launch shapes: the
+    default (small frontiers on one block or a 16-block sub-grid) and every
+    pass on the full grid with 4-lane row groups or a lane per short row."""
     from parity_checks import check_batch
     p = dlp.Problem(20_000_000, 7, 100, 42)
     orc = oracle.OracleRun.from_problem(p, record=True, threads=0)
     runs = [dlp.Session.from_problem(p, record=True),
-            dlp.Session.from_problem(p, record=True, small_frontier_solo=0, narrow_lanes=4)]
+            dlp.Session.from_problem(p, record=True, small_frontier_solo=0, narrow_lanes=4),
+            dlp.Session.from_problem(p, record=True, small_frontier_solo=0, narrow_lanes=1)]
     for b in range(ORACLE_BATCHES):
         want = orc.apply(b, p.batches[b])
         for sess in runs:

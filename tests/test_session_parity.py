@@ -23,6 +23,8 @@ CONFIGS = [
     (2000, 7, 6, 3, dlp.SEMANTICS_REF, 4),
     (3000, 4, 3, 11, dlp.SEMANTICS_REF, 16),
     (5000, 5, 10, 42, dlp.SEMANTICS_REF, 32),
+    (5000, 5, 10, 42, dlp.SEMANTICS_REF, 1),
+    (2000, 7, 6, 3, dlp.SEMANTICS_SPEC, 1),
     (5000, 5, 10, 42, dlp.SEMANTICS_SPEC, 8),
     (2000, 7, 6, 3, dlp.SEMANTICS_SPEC, 4),
     (50000, 5, 10, 42, dlp.SEMANTICS_REF, 8),
@@ -67,6 +69,7 @@ MODES = [
     dict(small_frontier_solo=3),                       # one-block passes without the 8-warp team
     dict(small_frontier_solo=1),                       # one-block only
     dict(small_frontier_solo=0),                       # every pass on the full grid
+    dict(small_frontier_solo=0, narrow_lanes=1),       # full grid, a lane per short row
     dict(solo_entry=1024, subgrid_entry=4096),         # the largest thresholds
     dict(solo_entry=256, subgrid_entry=1024, narrow_lanes=16),
 ]
@@ -77,8 +80,8 @@ MODES = [
 @pytest.mark.parametrize("n", [5000, 50000])
 def test_pass_modes_give_identical_results(gpu, sem, n):
     """The passes give the same results whichever mode runs them: the 8-warp
-    team, the one-block mode, the sub-grid, the full grid, at any
-    thresholds."""
+    team, the one-block mode, the sub-grid, the full grid (lane groups or a
+    lane per short row), at any thresholds."""
     p = dlp.Problem(n, 5, 10, 42)
     runs = [dlp.Session.from_problem(p, semantics=sem, **m) for m in MODES]
     for i, bt in enumerate(p.batches):
