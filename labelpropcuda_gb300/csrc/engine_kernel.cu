@@ -1486,7 +1486,9 @@ __device__ __forceinline__ void lane_mark(const GV &w, bool valid, int key, cons
   const int tail = 31 - __clz(peers);
   const int tot = __shfl_sync(0xffffffffu, incl, tail);
   int bn = 0, bw = 0, bf = 0;
-  if (lane == tail && valid && tot != 0) {
+  // the run's last lane reserves for the whole run, whether or not it marked
+  // anything itself (its own row may be one for the 4-lane groups)
+  if (lane == tail && tot != 0) {
     const int tn = tot & 1023, tw = (tot >> 10) & 1023, tf = tot >> 20;
     if (tn) bn = atomicAdd(&s.bc->front_count[set][0], tn);
     if (tw) bw = atomicAdd(&s.bc->front_count[set][1], tw);
