@@ -1533,7 +1533,13 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
       if (r.ba.record && kg < kRecordIters) r.st.rec_fsizes[kg] = nn + nw;
     }
   }
-  if constexpr (G == 1) {
+  // A frontier large enough to give every warp two or more rounds of G-lane
+  // groups runs with one lane per short row instead: 32 rows in flight per
+  // warp rather than 32 / G, so a warp's dependent memory round trips overlap
+  // across four to eight times more rows. Smaller frontiers keep the groups,
+  // which spread one row's entries over G lanes. Same results either way.
+  const bool lane_rows = G == 1 || tn >= 2 * nwarps * GPW;
+  if (lane_rows) {
     // rows of at most 32 entries: one lane per row of at most 8 entries, 32
     // rows in flight per warp; rows of 9 to 32 entries of the same 32 go to
     // 4-lane groups afterwards
