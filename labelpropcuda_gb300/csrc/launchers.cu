@@ -132,10 +132,20 @@ __global__ void sparsify_build(SparsifyArgs a, const int *block_counts, int *aff
   __shared__ int s_warp[kBlock / 32];
   __shared__ int s_base;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    int b = 0;
-    for (int k = 0; k < static_cast<int>(blockIdx.x); ++k) b += block_counts[k];
-    s_base = b;
+  // this block's first slot: the kept edges of the blocks before it, summed
+  // by the whole block (one load per thread per 1024 blocks, not a serial walk)
+  {
+    int part = 0;
+    for (int q = threadIdx.x; q < static_cast<int>(blockIdx.x); q += blockDim.x) part += block_counts[q];
+    part = __reduce_add_sync(0xffffffffu, part);
+    if (lane == 0) s_warp[wid] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int b = 0;
+      for (int q = 0; q < kBlock / 32; ++q) b += s_warp[q];
+      s_base = b;
+    }
+    __syncthreads();
   }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool bad = false;
