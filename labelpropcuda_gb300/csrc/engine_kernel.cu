@@ -1096,51 +1096,26 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
       }
     add = __reduce_add_sync(0xffffffffu, add);
     wide = __reduce_or_sync(0xffffffffu, wide);
-    if constexpr (R <= 8) {
-      // one ballot per candidate slot (independent, unlike a shuffle scan):
-      // the warp's fresh marks of slot r take a run of the reservation, in
-      // lane order
-      unsigned bal[R + 1];
-      int tot = 0;
+    // one reservation in the next list for the whole warp, by a scan of the
+    // per-lane counts
+    const int nf = __popc(fresh);
+    int incl = nf;
 #pragma unroll
-      for (int r = 0; r < R + 1; ++r) {
-        bal[r] = __ballot_sync(0xffffffffu, (fresh >> r) & 1u);
-        tot += __popc(bal[r]);
-      }
-      int at = 0;
-      if (lane == 0 && tot) {
-        at = atomicAdd(&c.cnt[nq], tot);
-        if (add) atomicAdd(&c.need[nq], add);
-        if (wide) c.wide[nq] = 1;
-      }
-      at = __shfl_sync(0xffffffffu, at, 0);
-      const unsigned below = (1u << lane) - 1u;
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r) {
-        if ((fresh >> r) & 1u) next[at + __popc(bal[r] & below)] = static_cast<unsigned short>(r < R ? vv[r] : su);
-        at += __popc(bal[r]);
-      }
-    } else {
-      // many slots per lane: a scan of the per-lane counts keeps fewer values live
-      const int nf = __popc(fresh);
-      int incl = nf;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const int tot = __shfl_sync(0xffffffffu, incl, 31);
-      int at = 0;
-      if (lane == 31 && tot) {
-        at = atomicAdd(&c.cnt[nq], tot);
-        if (add) atomicAdd(&c.need[nq], add);
-        if (wide) c.wide[nq] = 1;
-      }
-      at = __shfl_sync(0xffffffffu, at, 31) + incl - nf;
-#pragma unroll
-      for (int r = 0; r < R + 1; ++r)
-        if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
     }
+    const int tot = __shfl_sync(0xffffffffu, incl, 31);
+    int at = 0;
+    if (lane == 31 && tot) {
+      at = atomicAdd(&c.cnt[nq], tot);
+      if (add) atomicAdd(&c.need[nq], add);
+      if (wide) c.wide[nq] = 1;
+    }
+    at = __shfl_sync(0xffffffffu, at, 31) + incl - nf;
+#pragma unroll
+    for (int r = 0; r < R + 1; ++r)
+      if ((fresh >> r) & 1u) next[at++] = static_cast<unsigned short>(r < R ? vv[r] : su);
   }
 }
 
@@ -1150,8 +1125,8 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
 // block wait at the block barrier that ends the team stint. The passes and
 // their arithmetic are those of the whole block; only fewer warps share the
 // rows, and the waiting warps take no issue slots from them.
-constexpr int kTeamWarps = 8;
-constexpr int kTeamRows = kTeamWarps * 32 / 4;  // rows one round of 4-lane groups takes
+constexpr int kTeamWarps = 16;
+constexpr int kTeamRows = kTeamWarps * 32 / 4;  // rows one round of 4-lane groups takes (8 lanes up to 64)
 
 __device__ __forceinline__ void team_barrier() {
   asm volatile("bar.sync 1, %0;" ::"r"(kTeamWarps * 32) : "memory");
@@ -1165,16 +1140,22 @@ __device__ int team_passes(const EngineArgs &e, SoloCache &c, int k0, int k, int
                            uint64_t t0) {
   const int tid = threadIdx.x;
   const int ng = e.ng;
+  // The vertex table and the row pool do not grow during a team stint (it
+  // runs only while no row is left to load), so their limits are checked once.
+  if (c.used > kVTUse || c.rp_top > kRP) return k;
+  // the last pass any limit allows, and the list indices, kept incrementally
+  int last = min(max_iter, k0 + kSoloMaxPasses);
+  if (e.pass_budget > 0) last = min(last, e.pass_budget);
+  const unsigned long long t_launch = e.slice_ns ? ld_relaxed_u64(&e.ectl->t_launch) : 0;
+  int q = (k - k0) % 3;
   for (;; ++k) {
     const int j = k - k0;
-    const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
-    const int cnt = c.cnt[q];
-    const int need = c.need[q];
-    if (cnt == 0 || cnt > kTeamRows || need > 0 || c.wide[q] || k >= max_iter || j >= kSoloMaxPasses ||
-        j >= c.stop_at || (e.pass_budget > 0 && k >= e.pass_budget) || c.used > kVTUse || c.rp_top > kRP)
-      break;
+    const int nq = q == 2 ? 0 : q + 1, z = nq == 2 ? 0 : nq + 1, p = j & 1;
+    // every exit condition from values read together (no chain of
+    // short-circuit loads)
+    const int cnt = c.cnt[q], need = c.need[q], wide = c.wide[q], stop_at = c.stop_at;
+    if ((cnt == 0) | (cnt > kTeamRows) | (need > 0) | (wide != 0) | (k >= last) | (j >= stop_at)) break;
     if (tid == 0) {
-      const int z = (j + 2) % 3;
       c.cnt[z] = 0;
       c.need[z] = 0;
       c.wide[z] = 0;
@@ -1190,13 +1171,15 @@ __device__ int team_passes(const EngineArgs &e, SoloCache &c, int k0, int k, int
     if (cnt <= kTeamWarps * 4) solo_rows<8, kTeamWarps>(e, c, cur, next, cnt, nq, k, rec_any);
     else solo_rows<4, kTeamWarps>(e, c, cur, next, cnt, nq, k, rec_any);
     if (tid == 0 && (j & 15) == 15) {
-      if (global_timer_ns() - t0 > kSoloBudgetNs) c.stop_at = j + 1;
-      if (slice_over(e)) {
+      const uint64_t now = global_timer_ns();
+      if (now - t0 > kSoloBudgetNs) c.stop_at = j + 1;
+      if (e.slice_ns != 0 && now - t_launch > e.slice_ns) {  // slice_over without re-reading t_launch
         c.stop_at = j + 1;
         c.stop_slice = 1;
       }
     }
     team_barrier();
+    q = nq;
   }
   return k;
 }
@@ -1265,12 +1248,12 @@ __device__ void solo_passes(const EngineArgs &e, int k0, int slot, SoloCache &c)
   for (;; ++k) {
     const int j = k - k0;
     const int q = j % 3, nq = (j + 1) % 3, p = j & 1;
-    const int cnt = c.cnt[q];
-    const int need = c.need[q];
+    const int cnt = c.cnt[q], need = c.need[q], wide = c.wide[q], stop_at = c.stop_at, used = c.used,
+              rp_top = c.rp_top;
     // the same decision in every thread: its inputs were last written before
-    // the previous barrier
-    if (cnt == 0 || cnt > kSoloList || k >= max_iter || c.wide[q] || j >= kSoloMaxPasses || j >= c.stop_at ||
-        (e.pass_budget > 0 && k >= e.pass_budget) || c.used + need > kVTUse || c.rp_top + need > kRP)
+    // the previous barrier (all read together, no chain of short-circuit loads)
+    if ((cnt == 0) | (cnt > kSoloList) | (k >= max_iter) | (wide != 0) | (j >= kSoloMaxPasses) | (j >= stop_at) |
+        ((e.pass_budget > 0) & (k >= e.pass_budget)) | (used + need > kVTUse) | (rp_top + need > kRP))
       break;
     if (need == 0 && cnt <= kTeamRows && k >= team_from) {
       if (warp < kTeamWarps) {
