@@ -851,7 +851,12 @@ def main(argv=None) -> int:
     ap.add_argument("--per-batch", action="store_true", help="add every batch's statistics to the line")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's own CUDA build (oracle/_ref/ref_kernels)")
+    ap.add_argument("--input-cache", default=None,
+                    help="directory of the binary input cache (DLP_INPUT_CACHE): generated problems are kept there "
+                         "and read back on later runs")
     args = ap.parse_args(argv)
+    if args.input_cache:
+        os.environ["DLP_INPUT_CACHE"] = args.input_cache
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if "WORLD_SIZE" not in os.environ and args.gpus > 1:

@@ -94,6 +94,22 @@ int dlp_problem_batch(const dlp_problem *p, int batch, dlp_batch_view *out);
 /* <prefix>RowPtr.txt, ColInd.txt, Values.txt, TrueLabels.txt in the reference's
  * text format (src/generateSparseGraph.cu:224-271). */
 int dlp_problem_write_csr(const dlp_problem *p, const char *prefix);
+/* Binary input cache. The reference regenerates its input on every run and
+ * writes its graph only as text it never reads back
+ * (src/generateSparseGraph.cu:218-274); these keep a generated problem in one
+ * binary file keyed by the generator arguments.
+ * dlp_problem_save writes p to path (a temporary file, then a rename).
+ * dlp_problem_load reads a file written by dlp_problem_save; a file whose
+ * recorded size or payload hash does not match is refused.
+ * dlp_problem_generate_cached reads the file of these arguments from
+ * cache_dir when it is present and valid, else generates the problem (same
+ * output as dlp_problem_generate) and (re)writes the file; *from_cache (may be
+ * NULL) is 1 when the problem came from the file. */
+int dlp_problem_save(const dlp_problem *p, const char *path);
+int dlp_problem_load(const char *path, dlp_problem **out);
+int dlp_problem_generate_cached(int num_nodes, int avg_degree, int num_batches, unsigned seed,
+                                float gt_fraction, float deleted_fraction, const char *cache_dir,
+                                dlp_problem **out, int *from_cache);
 /* Mean weight of the non-deleted edges of a CSR (auto tau, src/dynLP.cu:90-102). */
 float dlp_mean_edge_weight(int64_t num_edges, const int *col_ind, const float *values);
 

@@ -11,7 +11,9 @@ package wraps its C ABI for tests, benchmarks and Python callers:
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
+from pathlib import Path
 
 import numpy as np
 
@@ -65,14 +67,45 @@ class Batch:
 
 class Problem:
     """Seeded synthetic input: full CSR graph, true labels and the batch list,
-    identical to the reference generator's output for the same arguments."""
+    identical to the reference generator's output for the same arguments.
+
+    cache_dir (default: the DLP_INPUT_CACHE environment variable; none when
+    unset or empty) keeps the generated problem in a binary file there, keyed
+    by the arguments, and reads it back on the next construction instead of
+    generating again (dlp_problem_generate_cached). `from_cache` says which
+    happened. Problem.load(path) reads such a file directly."""
 
     def __init__(self, num_nodes: int, avg_degree: int, num_batches: int, seed: int = 42,
-                 gt_fraction: float = 0.01, deleted_fraction: float = 0.09):
+                 gt_fraction: float = 0.01, deleted_fraction: float = 0.09, cache_dir: str | None = None):
         L = _n.lib()
         h = ctypes.c_void_p()
-        _n.check(L.dlp_problem_generate(num_nodes, avg_degree, num_batches, seed, gt_fraction, deleted_fraction,
-                                        ctypes.byref(h)))
+        cache_dir = os.environ.get("DLP_INPUT_CACHE") if cache_dir is None else cache_dir
+        self.from_cache = False
+        if cache_dir:
+            Path(cache_dir).mkdir(parents=True, exist_ok=True)
+            hit = ctypes.c_int(0)
+            _n.check(L.dlp_problem_generate_cached(num_nodes, avg_degree, num_batches, seed, gt_fraction,
+                                                   deleted_fraction, str(cache_dir).encode(), ctypes.byref(h),
+                                                   ctypes.byref(hit)))
+            self.from_cache = bool(hit.value)
+        else:
+            _n.check(L.dlp_problem_generate(num_nodes, avg_degree, num_batches, seed, gt_fraction,
+                                            deleted_fraction, ctypes.byref(h)))
+        self._take(h)
+
+    @classmethod
+    def load(cls, path: str | os.PathLike) -> "Problem":
+        """A problem read from a cache file (dlp_problem_load: size and hash checked)."""
+        L = _n.lib()
+        h = ctypes.c_void_p()
+        _n.check(L.dlp_problem_load(str(path).encode(), ctypes.byref(h)))
+        self = cls.__new__(cls)
+        self.from_cache = True
+        self._take(h)
+        return self
+
+    def _take(self, h: ctypes.c_void_p) -> None:
+        L = _n.lib()
         try:
             self.num_nodes = L.dlp_problem_num_nodes(h)
             m = L.dlp_problem_num_edges(h)

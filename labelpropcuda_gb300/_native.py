@@ -127,6 +127,10 @@ _SIGNATURES = {
     "dlp_problem_true_labels": (_P, [_P]),
     "dlp_problem_batch": (_I, [_P, _I, ctypes.POINTER(BatchView)]),
     "dlp_problem_write_csr": (_I, [_P, ctypes.c_char_p]),
+    "dlp_problem_save": (_I, [_P, ctypes.c_char_p]),
+    "dlp_problem_load": (_I, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "dlp_problem_generate_cached": (_I, [_I, _I, _I, ctypes.c_uint, ctypes.c_float, ctypes.c_float, ctypes.c_char_p,
+                                         ctypes.POINTER(_P), ctypes.POINTER(_I)]),
     "dlp_mean_edge_weight": (ctypes.c_float, [ctypes.c_int64, _P, _P]),
     "dlp_config_default": (None, [ctypes.POINTER(Config)]),
     "dlp_session_create": (_I, [ctypes.POINTER(Config), _I, ctypes.c_int64, _P, _P, _P, _P, _P, ctypes.POINTER(_P)]),

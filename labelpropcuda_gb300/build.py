@@ -34,7 +34,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wa
              f"-I{INCLUDE}", f"-I{CSRC}"]
 
 CU_SOURCES = ["api.cu", "engine.cu", "engine_kernel.cu", "launchers.cu", "server.cu", "tune.cu"]
-CXX_SOURCES = ["host/generate.cpp", "shims.cpp"]
+CXX_SOURCES = ["host/generate.cpp", "host/problem_cache.cpp", "shims.cpp"]
 CLI_SOURCES = ["cli/main.cpp"]
 
 

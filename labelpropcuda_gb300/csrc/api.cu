@@ -56,7 +56,24 @@ int launch_cooperative(const void *kernel, int grid, int block, void **args, siz
 
 struct dlp_problem {
   dlp::Problem p;
+  dlp::ProblemKey key{};  // the generator arguments (the cache key)
 };
+
+namespace {
+
+dlp::ProblemKey problem_key(int n, int deg, int nb, unsigned seed, float gt, float del) {
+  dlp::ProblemKey k{};
+  k.num_nodes = n;
+  k.avg_degree = deg;
+  k.num_batches = nb;
+  k.seed = seed;
+  std::memcpy(&k.gt_fraction_bits, &gt, 4);
+  std::memcpy(&k.deleted_fraction_bits, &del, 4);
+  k.generator = dlp::kGeneratorVersion;
+  return k;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -86,6 +103,7 @@ int dlp_problem_generate(int num_nodes, int avg_degree, int num_batches, unsigne
   if (!(gt_fraction > 0.0f && gt_fraction < 1.0f))
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "gt_fraction must be in (0, 1)");
   dlp_problem *p = new dlp_problem();
+  p->key = problem_key(num_nodes, avg_degree, num_batches, seed, gt_fraction, deleted_fraction);
   std::string err;
   if (!dlp::generate_graph(num_nodes, avg_degree, seed, p->p.graph, p->p.truth, &err) ||
       !dlp::generate_batches(p->p.graph, p->p.truth, num_batches, seed, gt_fraction,
@@ -94,6 +112,55 @@ int dlp_problem_generate(int num_nodes, int avg_degree, int num_batches, unsigne
     return dlp::fail(DLP_ERR_INVALID_ARGUMENT, err);
   }
   *out = p;
+  return DLP_OK;
+}
+
+int dlp_problem_save(const dlp_problem *p, const char *path) {
+  dlp::clear_error();
+  if (!p || !path) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+  std::string err;
+  if (!dlp::save_problem(p->p, p->key, path, &err)) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, err);
+  return DLP_OK;
+}
+
+int dlp_problem_load(const char *path, dlp_problem **out) {
+  dlp::clear_error();
+  if (!path || !out) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  dlp_problem *p = new dlp_problem();
+  std::string err;
+  if (!dlp::load_problem(path, nullptr, p->p, &p->key, &err)) {
+    delete p;
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, err);
+  }
+  *out = p;
+  return DLP_OK;
+}
+
+int dlp_problem_generate_cached(int num_nodes, int avg_degree, int num_batches, unsigned seed, float gt_fraction,
+                                float deleted_fraction, const char *cache_dir, dlp_problem **out, int *from_cache) {
+  dlp::clear_error();
+  if (!out || !cache_dir || !*cache_dir) return dlp::fail(DLP_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (from_cache) *from_cache = 0;
+  const dlp::ProblemKey key = problem_key(num_nodes, avg_degree, num_batches, seed, gt_fraction, deleted_fraction);
+  const std::string path = std::string(cache_dir) + "/" + dlp::cache_file_name(key);
+  dlp_problem *p = new dlp_problem();
+  std::string err;
+  if (dlp::load_problem(path, &key, p->p, &p->key, &err)) {
+    *out = p;
+    if (from_cache) *from_cache = 1;
+    return DLP_OK;
+  }
+  delete p;
+  // absent, stale or damaged: generate, then (re)write the file
+  const int st = dlp_problem_generate(num_nodes, avg_degree, num_batches, seed, gt_fraction, deleted_fraction, out);
+  if (st != DLP_OK) return st;
+  if (!dlp::save_problem((*out)->p, key, path, &err)) {
+    dlp_problem_free(*out);
+    *out = nullptr;
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, err);
+  }
   return DLP_OK;
 }
 

@@ -60,4 +60,28 @@ bool write_csr_files(const HostGraph &g, const std::vector<float> &truth,
 // empty graph (src/dynLP.cu:90-102).
 float mean_edge_weight(const HostGraph &g);
 
+// Generator arguments that identify a problem in the binary cache. Fractions
+// are kept as their float bits; `generator` is kGeneratorVersion, raised
+// whenever the generator's decisions change so that older files are not used.
+constexpr uint32_t kGeneratorVersion = 1;
+struct ProblemKey {
+  int32_t num_nodes;
+  int32_t avg_degree;
+  int32_t num_batches;
+  uint32_t seed;
+  uint32_t gt_fraction_bits;
+  uint32_t deleted_fraction_bits;
+  uint32_t generator;
+  uint32_t reserved;
+};
+
+// File name of a key inside a cache directory.
+std::string cache_file_name(const ProblemKey &key);
+// Writes the problem to `path` (atomically: a temporary file, then a rename).
+bool save_problem(const Problem &p, const ProblemKey &key, const std::string &path, std::string *err);
+// Reads a problem written by save_problem. With `want`, a file of another key
+// is refused; every file is checked against its recorded size and hash.
+bool load_problem(const std::string &path, const ProblemKey *want, Problem &p, ProblemKey *key_out,
+                  std::string *err);
+
 }  // namespace dlp
