@@ -283,6 +283,53 @@ def fp64_error(problem, gpu_labels, threads: int) -> dict:
             "how": "oracle fp32 schedule vs the same batch's propagation in double from the same state"}
 
 
+def irlp_block(p, batch_ms: list, threads: int, budget_s: float, device: int) -> dict:
+    """IrLP full recompute after every batch of the workload, on the snapshot
+    the reference's driver builds for it (src/main.cu:127-176): on the GPU
+    (dlp_irlp, one cooperative launch per snapshot, the whole run) and on the
+    host cores (the oracle's restatement of src/validation.cu:47-139, all
+    threads; per snapshot a bounded number of iterations, scaled to the GPU's
+    iteration count when the budget does not cover the whole run), beside the
+    incremental path's per-batch device time."""
+    import numpy as np
+    import labelpropcuda_gb300 as dlp
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    snaps = [dlp.irlp_snapshot(p, b) for b in range(len(p.batches))]
+    dlp.irlp(snaps[-1], max_iterations=10, device=device)  # first launch: module load
+    rows, per_snap_s = [], budget_s / max(1, len(snaps))
+    for b, snap in enumerate(snaps):
+        t = {}
+        lab, it = dlp.irlp(snap, device=device, timing=t)
+        visits = it * int(np.diff(snap.row_ptr)[snap.status == 0].sum())
+        # CPU: a probe of a few iterations sets how many fit this snapshot's share
+        t0 = time.perf_counter()
+        _, k0, _ = pyoracle.irlp(snap.num_nodes, snap.row_ptr, snap.col_ind, snap.values, snap.status,
+                                 snap.gt_class, snap.labels, max_iterations=min(it, 5) or 1, threads=threads)
+        per_it = (time.perf_counter() - t0) / max(k0, 1)
+        k = max(1, min(it, int(per_snap_s / max(per_it, 1e-9))))
+        t0 = time.perf_counter()
+        cl, kc, _ = pyoracle.irlp(snap.num_nodes, snap.row_ptr, snap.col_ind, snap.values, snap.status,
+                                     snap.gt_class, snap.labels, max_iterations=k, threads=threads)
+        cpu_s = time.perf_counter() - t0
+        whole = kc >= it
+        rows.append({"batch": b, "iterations": it, "edge_visits": visits, "gpu_ms": t["ms"],
+                     "cpu_ms": 1e3 * (cpu_s if whole else cpu_s / max(kc, 1) * it),
+                     "cpu_iterations_timed": kc, "cpu_estimated": not whole,
+                     "labels_equal_cpu": bool(np.array_equal(cl, lab)) if whole else None,
+                     "incremental_ms": batch_ms[b]})
+    gpu_ms = sum(r["gpu_ms"] for r in rows)
+    inc_ms = sum(batch_ms)
+    return {"snapshot": "the driver's IrLP input after each batch (src/main.cu:127-176)",
+            "gpu_ms_all_batches": gpu_ms, "cpu_ms_all_batches": sum(r["cpu_ms"] for r in rows),
+            "incremental_ms_all_batches": inc_ms,
+            "gpu_irlp_over_incremental": gpu_ms / inc_ms if inc_ms > 0 else None,
+            "gpu_edge_visits_per_s": sum(r["edge_visits"] for r in rows) / (gpu_ms / 1e3) if gpu_ms > 0 else None,
+            "cpu_threads": threads, "cpu_kind": "oracle port",
+            "timing": "GPU: wall time of one dlp_irlp launch, device synchronised on both sides, inputs resident; "
+                      "CPU: wall time", "per_batch": rows}
+
+
 def reference_cuda(w: dict, batches: int, our_stats: list) -> dict | None:
     """The reference's own CUDA build (its runDynLP, launchers and kernels,
     -O3 --use_fast_math, from the guarded source copy) timed on this GPU on
@@ -453,6 +500,10 @@ def gpu_arm(args, td, rank, world, local_rank):
     if not args.no_fp64:
         progress("fp64 oracle")
         fp64 = fp64_error(p, sess.labels(), cpu["nproc"])
+    irlp_full = None
+    if not args.no_irlp:
+        progress("IrLP full recompute")
+        irlp_full = irlp_block(p, [s["device_ms"] for s in stats0], cpu["nproc"], args.irlp_budget_s, local_rank)
     ref_cuda = None
     if not args.no_reference_cuda:
         progress("reference CUDA build")
@@ -482,6 +533,7 @@ def gpu_arm(args, td, rank, world, local_rank):
                          "sample": f"oracle port, 1 thread, first {cpu_done} of {nb} batches of the same workload",
                          "cpu_model": cpu["model"], "host_cores": cpu["nproc"]},
         "fp64_oracle_error": fp64,
+        "irlp_full_recompute": irlp_full,
         "reference_cuda": ref_cuda,
         "clocks": clocks,
         "pass_modes_per_step": modes,
@@ -848,6 +900,8 @@ def main(argv=None) -> int:
     ap.add_argument("--plain-per-stratum", type=int, default=3)
     ap.add_argument("--plain-strata", type=int, default=8)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 oracle error of the headline workload")
+    ap.add_argument("--no-irlp", action="store_true", help="skip the IrLP full-recompute comparison")
+    ap.add_argument("--irlp-budget-s", type=float, default=10.0, help="host time for the CPU IrLP leg")
     ap.add_argument("--per-batch", action="store_true", help="add every batch's statistics to the line")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's own CUDA build (oracle/_ref/ref_kernels)")

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import time
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -20,8 +21,8 @@ import numpy as np
 from . import _native as _n
 from ._native import DlpError, SEMANTICS_REF, SEMANTICS_SPEC, ARITH_IEEE, ARITH_REFERENCE_FAST_MATH  # noqa: F401
 
-__all__ = ["Problem", "Session", "DeviceArray", "DlpError", "SEMANTICS_REF", "SEMANTICS_SPEC",
-           "device_count", "batch_map"]
+__all__ = ["Problem", "Session", "DeviceArray", "IrlpSnapshot", "irlp_snapshot", "irlp", "DlpError",
+           "SEMANTICS_REF", "SEMANTICS_SPEC", "device_count", "batch_map"]
 
 
 def _ptr(a: np.ndarray | None) -> int | None:
@@ -142,6 +143,74 @@ def batch_map(num_nodes: int, batches: list[Batch]) -> np.ndarray:
     for b, bt in enumerate(batches):
         m[bt.inserted] = b
     return m
+
+
+@dataclass
+class IrlpSnapshot:
+    """The IrLP full-recompute input for the graph as it stands after a batch."""
+    row_ptr: np.ndarray      # int32, n + 1: active rows, active neighbours, in CSR order
+    col_ind: np.ndarray      # int32
+    values: np.ndarray       # float32
+    status: np.ndarray       # int32 per vertex: 0 active, 1 deleted (or not yet inserted), 2 ground truth
+    gt_class: np.ndarray     # int32 per vertex: 0 / 1 for ground truth, -1 otherwise
+    labels: np.ndarray       # float32 per vertex: the ground-truth label, 0.5 otherwise
+
+    @property
+    def num_nodes(self) -> int:
+        return int(self.status.size)
+
+
+def irlp_snapshot(p: "Problem", last_batch: int | None = None) -> IrlpSnapshot:
+    """The snapshot the reference's driver hands to its IrLP baseline
+    (src/main.cu:127-176), after batch `last_batch` (default: the last one):
+    every vertex starts deleted; batch by batch, inserted vertices become
+    active, deleted ones deleted, ground-truth ones ground truth with their
+    class and label; the CSR keeps, for each live inserted vertex, its live
+    inserted neighbours in the full graph's order."""
+    n = p.num_nodes
+    upto = len(p.batches) if last_batch is None else last_batch + 1
+    status = np.full(n, 1, np.int32)
+    gt = np.full(n, -1, np.int32)
+    lab = np.full(n, 0.5, np.float32)
+    inserted = np.zeros(n, bool)
+    for bt in p.batches[:upto]:
+        status[bt.inserted] = 0
+        inserted[bt.inserted] = True
+        status[bt.deleted] = 1
+        status[bt.gt_ids] = 2
+        gt[bt.gt_ids] = np.where(bt.gt_labels < 0.5, 0, 1)
+        lab[bt.gt_ids] = bt.gt_labels
+    live = (status != 1) & inserted
+    rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(p.row_ptr).astype(np.int64))
+    col = p.col_ind
+    keep = live[rows] & (col >= 0)
+    keep[keep] &= live[col[keep]]
+    counts = np.bincount(rows[keep], minlength=n)
+    row_ptr = np.zeros(n + 1, np.int64)
+    np.cumsum(counts, out=row_ptr[1:])
+    return IrlpSnapshot(row_ptr.astype(np.int32), col[keep].astype(np.int32), p.values[keep].astype(np.float32),
+                        status, gt, lab)
+
+
+def irlp(snap: IrlpSnapshot, delta: float = 1e-4, max_iterations: int = 100000, device: int = 0,
+         timing: dict | None = None) -> tuple[np.ndarray, int]:
+    """IrLP full recompute on the GPU (dlp_irlp, one cooperative launch; the
+    reference's launchIrLP, src/validation.cu:145-208). Returns the labels and
+    the iterations used. With `timing`, timing["ms"] is the launch's wall
+    time, device synchronised on both sides, inputs already on the device."""
+    L = _n.lib()
+    _n.check(L.dlp_set_device(device))
+    d = [DeviceArray(x) for x in (snap.row_ptr, snap.col_ind, snap.values, snap.labels, snap.status,
+                                  snap.gt_class)]
+    it = ctypes.c_int(0)
+    _n.check(L.dlp_device_synchronize())
+    t0 = time.perf_counter()
+    _n.check(L.dlp_irlp(d[0].ptr, d[1].ptr, d[2].ptr, d[3].ptr, d[4].ptr, d[5].ptr, snap.num_nodes,
+                        ctypes.c_float(delta), max_iterations, ctypes.byref(it), None))
+    _n.check(L.dlp_device_synchronize())
+    if timing is not None:
+        timing["ms"] = 1e3 * (time.perf_counter() - t0)
+    return d[3].get(), it.value
 
 
 class Session:
