@@ -1526,11 +1526,32 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
     // rows of at most 32 entries: one lane per row of at most 8 entries, 32
     // rows in flight per warp; rows of 9 to 32 entries of the same 32 go to
     // 4-lane groups afterwards
-    for (int base = warp0 * 32; base < tn; base += nwarps * 32) {
+    // A lane's row of the next round is looked up while this round's rows
+    // are in flight: its frontier entry is loaded at the top of the round,
+    // its row start and length once this round's gathers are done. The
+    // frontier list and the row table do not change during a pass.
+    const int stride = nwarps * 32;
+    auto entry_of = [&](int item, int &g, int &u) {
+      g = 0;
+      u = 0;
+      if (item < tn) {
+        g = locate(pref, ng, item);
+        const GraphRec &r = e.recs[g];
+        u = r.st.flist[static_cast<size_t>((k + r.ba.pass0) % 3) * r.st.n + (item - pref[g])];
+      }
+    };
+    int g, u, rs = 0, len = 0;
+    entry_of(warp0 * 32 + lane, g, u);
+    if (warp0 * 32 + lane < tn) {
+      const int2 ri = e.recs[g].st.rowinfo[u];
+      rs = ri.x;
+      len = ri.y;
+    }
+    for (int base = warp0 * 32; base < tn; base += stride) {
       const int item = base + lane;
       const bool valid = item < tn;
-      const int g = valid ? locate(pref, ng, item) : 0;
-      int u = 0, rs = 0, len = 0;
+      int g1, u1, rs1 = 0, len1 = 0;
+      entry_of(item + stride, g1, u1);
       {
         const GV w = view(e, g);
         const DevState &s = w.s;
@@ -1538,30 +1559,38 @@ __device__ void run_pass(const EngineArgs &e, int k, const int *pref, int tn, co
         const int cb = s.ctl->cur_buf;
         const float *src = ((cb ^ kg) & 1) ? s.lab1 : s.lab0;
         float *dst = ((cb ^ kg) & 1) ? s.lab0 : s.lab1;
-        if (valid) {
-          u = s.flist[static_cast<size_t>(kg % 3) * s.n + (item - pref[g])];
-          const int2 ri = s.rowinfo[u];
-          rs = ri.x;
-          len = ri.y;
-        }
         const bool mine = valid && len <= kLaneRow;
         int cand[kLaneRow + 1];
         unsigned wide_bits = 0;
         lane_row(s, src, dst, w.a.delta, e.fast_div, u, rs, len, mine, cand, wide_bits);
+        if (item + stride < tn) {
+          const int2 ri = e.recs[g1].st.rowinfo[u1];
+          rs1 = ri.x;
+          len1 = ri.y;
+        }
         lane_mark(w, mine, valid ? g : -1, cand, wide_bits, w.g0 + static_cast<unsigned>(kg) + 1u, (kg + 1) % 3,
                   lane);
         add_keyed(mine, static_cast<unsigned>(len), &s.bc->aff_edges);
         add_keyed(mine, 1u, &s.bc->front_visits);
+        // the 4-lane groups below take this round's long rows
+        const int gc = g, uc = u, lc = len;
+        g = g1;
+        u = u1;
+        rs = rs1;
+        len = len1;
+        g1 = gc;
+        u1 = uc;
+        len1 = lc;
       }
-      unsigned longm = __ballot_sync(0xffffffffu, valid && len > kLaneRow);
+      unsigned longm = __ballot_sync(0xffffffffu, valid && len1 > kLaneRow);
       const int q = lane >> 2, ql = lane & 3;
       while (longm) {  // up to 8 rows a round, the q-th remaining one to 4-lane group q
         unsigned m = longm;
         for (int i = 0; i < q && m; ++i) m &= m - 1;
         const bool have = m != 0;
         const int from = have ? __ffs(m) - 1 : 0;
-        const int gq = __shfl_sync(0xffffffffu, g, from);
-        const int uq = __shfl_sync(0xffffffffu, u, from);
+        const int gq = __shfl_sync(0xffffffffu, g1, from);
+        const int uq = __shfl_sync(0xffffffffu, u1, from);
         for (int i = 0; i < 8 && longm; ++i) longm &= longm - 1;
         const GV w = view(e, gq);
         const DevState &s = w.s;
