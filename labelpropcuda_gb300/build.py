@@ -1,11 +1,10 @@
 """In-tree build of the GB300 DynLP library (no cmake, no setuptools).
 
-    python -m labelpropcuda_gb300.build          # library + CLI
+    python -m labelpropcuda_gb300.build          # the library
     python -m labelpropcuda_gb300.build --verbose-ptxas
 
 Produces labelpropcuda_gb300/_build/libdynlp_gb300.so (C ABI, include/dlp_gb300.h
-plus the reference-signature C++ shims) and the drop-in CLI
-labelpropcuda_gb300/_build/dynlp_gb300. Device code is compiled for sm_103a only.
+plus the reference-signature C++ shims). Device code is compiled for sm_103a only.
 """
 from __future__ import annotations
 
@@ -22,7 +21,6 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
 LIB = BUILD / "libdynlp_gb300.so"
-CLI = BUILD / "dynlp_gb300"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -35,7 +33,6 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wa
 
 CU_SOURCES = ["api.cu", "engine.cu", "engine_kernel.cu", "launchers.cu", "server.cu", "tune.cu"]
 CXX_SOURCES = ["host/generate.cpp", "host/problem_cache.cpp", "shims.cpp"]
-CLI_SOURCES = ["cli/main.cpp"]
 
 
 def _nvcc() -> str:
@@ -94,10 +91,6 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> Path:
             f.result()
     if force or _stale(LIB, objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp"])
-    cli_srcs = [CSRC / s for s in CLI_SOURCES]
-    if all(p.exists() for p in cli_srcs) and (force or _stale(CLI, cli_srcs + [LIB] + hdrs)):
-        _run([cxx, *CXX_FLAGS, *map(str, cli_srcs), "-o", str(CLI), f"-L{BUILD}", "-ldynlp_gb300",
-              f"-Wl,-rpath,{BUILD}", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 
