@@ -363,7 +363,7 @@ struct PropArgs {
   unsigned *stamp;     // n, zeroed
   int *lists;          // 3n
   int *counts;         // [3][2]
-  int *out;            // [0] passes, [1] last mark stamp
+  int *out;            // [0] passes, [1] last mark stamp, [2] next pass after a block-0 stint
   GridBarrier *bar;
   int *err;
   unsigned long long timeout_ns;
@@ -396,16 +396,10 @@ __global__ void __launch_bounds__(kBlock) prop_kernel(PropArgs a) {
 
   constexpr int GPW = 32 / G;
   const int grp = lane / G, gl = lane & (G - 1);
-  int k = 0;
-  for (;; ++k) {
+  // The rows of pass k (nn narrow, nw wide in list k % 3) by the warps
+  // [w0, w0 + nws) of the launch; marks go to list (k + 1) % 3.
+  auto rows = [&](int k, int nn, int nw, int w0, int nws) {
     const int set = k % 3;
-    const int nn = ld_relaxed_i32(&a.counts[2 * set]);
-    const int nw = ld_relaxed_i32(&a.counts[2 * set + 1]);
-    if (nn + nw == 0 || k >= a.max_iter) break;
-    if (t == 0) {
-      a.counts[2 * ((k + 2) % 3)] = 0;
-      a.counts[2 * ((k + 2) % 3) + 1] = 0;
-    }
     const float *src = (k & 1) ? a.buffer : a.labels;
     float *dst = (k & 1) ? a.labels : a.buffer;
     const unsigned stamp = static_cast<unsigned>(k) + 1u;
@@ -416,7 +410,7 @@ __global__ void __launch_bounds__(kBlock) prop_kernel(PropArgs a) {
       if (cand) fresh = atomicMax(&a.stamp[v], stamp) < stamp;
       append(fresh && a.status[v] == kActive && a.gt[v] < 0, v, nset);
     };
-    for (int base = gwarp * GPW; base < nn; base += nwarps * GPW) {
+    for (int base = w0 * GPW; base < nn; base += nws * GPW) {
       const int item = base + grp;
       const bool valid = item < nn;
       int u = 0, rs = 0, len = 0;
@@ -445,7 +439,7 @@ __global__ void __launch_bounds__(kBlock) prop_kernel(PropArgs a) {
       for (int r = 0; r < 32 / G; ++r) mark(changed && cols[r] >= 0 && a.gt[cols[r]] < 0, cols[r]);
       mark(changed && gl == 0 && a.gt[u] < 0, u);
     }
-    for (int wi = gwarp; wi < nw; wi += nwarps) {
+    for (int wi = w0; wi < nw; wi += nws) {
       const int u = cur[n - 1 - wi];
       const int rs = a.row_ptr[u], len = a.row_ptr[u + 1] - rs;
       auto load = [&](int e, int &v, float &w) {
@@ -473,7 +467,56 @@ __global__ void __launch_bounds__(kBlock) prop_kernel(PropArgs a) {
         mark(lane == 0 && a.gt[u] < 0, u);
       }
     }
+  };
+  // A frontier of narrow rows that one block takes in one round runs on
+  // block 0 alone, pass after pass with block barriers, while the other
+  // blocks wait at the next grid barrier: a pass then costs a block barrier
+  // instead of a grid barrier. The stint ends when the frontier empties,
+  // outgrows one round or gets a wide row, at maxIter, or after 100 ms (the
+  // waiting blocks' barrier has a 2 s limit); block 0 publishes the next pass.
+  constexpr int kSmallFront = kBlock / G;
+  __shared__ int s_stop;
+  int k = 0;
+  for (;;) {
+    const int set = k % 3;
+    const int nn = ld_relaxed_i32(&a.counts[2 * set]);
+    const int nw = ld_relaxed_i32(&a.counts[2 * set + 1]);
+    if (nn + nw == 0 || k >= a.max_iter) break;
+    if (nw == 0 && nn <= kSmallFront) {
+      if (blockIdx.x == 0) {
+        const int warp = threadIdx.x >> 5;
+        const uint64_t t_start = global_timer_ns();
+        if (threadIdx.x == 0) s_stop = 0;
+        __syncthreads();
+        for (;;) {
+          const int cs = k % 3;
+          const int cn = ld_relaxed_i32(&a.counts[2 * cs]);
+          const int cw = ld_relaxed_i32(&a.counts[2 * cs + 1]);
+          // the same decision in every thread: all inputs were written
+          // before the last block barrier
+          if (cn + cw == 0 || cw != 0 || cn > kSmallFront || k >= a.max_iter || s_stop) break;
+          if (threadIdx.x == 0) {
+            a.counts[2 * ((k + 2) % 3)] = 0;
+            a.counts[2 * ((k + 2) % 3) + 1] = 0;
+            if ((k & 15) == 15 && global_timer_ns() - t_start > 100000000ull) s_stop = 1;
+          }
+          rows(k, cn, 0, warp, kBlock / 32);
+          __syncthreads();
+          ++k;
+        }
+        if (threadIdx.x == 0) a.out[2] = k;
+      }
+      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+      k = ld_relaxed_i32(&a.out[2]);
+      continue;
+    }
+    if (t == 0) {
+      a.counts[2 * ((k + 2) % 3)] = 0;
+      a.counts[2 * ((k + 2) % 3) + 1] = 0;
+    }
+    rows(k, nn, nw, gwarp, nwarps);
     if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+    ++k;
   }
   // final labels in the primary array, ground truth enforced
   // (src/iterativePropagation.cu:330-339); isAffected holds the last pass's marks
