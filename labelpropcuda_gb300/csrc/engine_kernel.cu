@@ -946,14 +946,13 @@ constexpr int kSoloG = DLP_SOLO_LANES;  // lanes per row in the one-block passes
 struct SoloCache {
   unsigned long long key[kVT];   // (graph << 32) | vertex, kEmptyKey = free
   float lab[2][kVT];             // the graph's physical buffers 0 and 1
-  int mark[kVT];                 // last pass (+1) that put the slot in the next frontier
+  int mark[kVT];                 // last pass (+1) that put the slot in the next frontier; INT_MAX: ground truth
   unsigned short row[kVT];       // row-pool offset, kNoRow = not loaded
   unsigned short visits[kVT];    // passes of the stint that updated the slot
   int2 rp[kRP];                  // {neighbour slot or -1, weight bits}
   unsigned short list[2][kSoloList];
   unsigned short graph[kVT];
   unsigned char len[kVT];        // live row length, kWideLen when longer than 32
-  signed char gt[kVT];
   unsigned char flags[kVT];      // bit0 written, bit1 in a frontier, bit2 buffer read at stint pass 0
   int lastpass[kMaxGraphs];      // last launch pass each graph took part in during the stint
   // Per list, indexed by stint pass % 3: the list read by pass j is filled
@@ -987,14 +986,13 @@ __device__ __forceinline__ int vt_slot(SoloCache &c, const EngineArgs &e, int g,
       const DevState &s = e.recs[g].st;
       c.lab[0][h] = s.lab0[v];
       c.lab[1][h] = s.lab1[v];
-      c.gt[h] = s.gt[v];
       const int len = s.act_len[v];
       c.len[h] = len > kNarrowMax ? kWideLen : static_cast<unsigned char>(len);
       c.graph[h] = static_cast<unsigned short>(g);
       c.flags[h] = static_cast<unsigned char>(((s.ctl->cur_buf ^ e.recs[g].ba.pass0) & 1) << 2);
       c.row[h] = kNoRow;
       c.visits[h] = 0;
-      c.mark[h] = -1;
+      c.mark[h] = s.gt[v] < 0 ? -1 : 0x7fffffff;  // a ground-truth slot is never marked
       atomicAdd(&c.used, 1);
       return static_cast<int>(h);
     }
@@ -1082,7 +1080,7 @@ __device__ __forceinline__ void solo_rows(const EngineArgs &e, SoloCache &c, con
 #pragma unroll
       for (int r = 0; r < R + 1; ++r) {
         const int ns = r < R ? vv[r] : ((gl == 0 && valid) ? su : -1);
-        if (ns >= 0 && c.gt[ns] < 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
+        if (ns >= 0 && atomicMax(&c.mark[ns], k + 1) < k + 1) fresh |= 1u << r;
       }
     }
     int add = 0, wide = 0;
