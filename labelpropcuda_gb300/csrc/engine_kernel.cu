@@ -913,8 +913,8 @@ __device__ __forceinline__ unsigned long long stop_code(const EngineArgs &e, int
 // Solo mode: when all graphs' frontiers together are small, block 0 runs the
 // passes alone with __syncthreads() between them while the other blocks wait
 // at the next grid barrier. The vertices the passes touch are held in shared
-// memory for the whole stint: a vertex table (both label buffers, class, row
-// length) for the frontier vertices and their neighbours, and a row pool with
+// memory for the whole stint: a vertex table (both label buffers, row
+// length, mark) for the frontier vertices and their neighbours, and a row pool with
 // each frontier row's entries as (table slot, weight). A row is loaded from
 // HBM the first time its vertex is in the frontier; afterwards a pass touches
 // only shared memory. Labels of vertices outside the frontier cannot change
