@@ -503,7 +503,11 @@ def gpu_arm(args, td, rank, world, local_rank):
     irlp_full = None
     if not args.no_irlp:
         progress("IrLP full recompute")
-        irlp_full = irlp_block(p, [s["device_ms"] for s in stats0], cpu["nproc"], args.irlp_budget_s, local_rank)
+        try:
+            irlp_full = irlp_block(p, [s["device_ms"] for s in stats0], cpu["nproc"], args.irlp_budget_s,
+                                   local_rank)
+        except Exception as exc:  # reported, not fatal: it is a baseline
+            irlp_full = {"error": repr(exc)[:300]}
     ref_cuda = None
     if not args.no_reference_cuda:
         progress("reference CUDA build")
