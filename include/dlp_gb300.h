@@ -103,8 +103,9 @@ int dlp_problem_write_csr(const dlp_problem *p, const char *prefix);
  * recorded size or payload hash does not match is refused.
  * dlp_problem_generate_cached reads the file of these arguments from
  * cache_dir when it is present and valid, else generates the problem (same
- * output as dlp_problem_generate) and (re)writes the file; *from_cache (may be
- * NULL) is 1 when the problem came from the file. */
+ * output as dlp_problem_generate) and (re)writes the file (cache_dir is
+ * created when missing; its parent must exist); *from_cache (may be NULL) is
+ * 1 when the problem came from the file. */
 int dlp_problem_save(const dlp_problem *p, const char *path);
 int dlp_problem_load(const char *path, dlp_problem **out);
 int dlp_problem_generate_cached(int num_nodes, int avg_degree, int num_batches, unsigned seed,

@@ -1,8 +1,11 @@
 // C ABI plumbing: error reporting, device checks, the problem (input
 // generation) object and small device helpers for bindings.
+#include <cerrno>
 #include <cstdio>
 #include <cstring>
 #include <string>
+
+#include <sys/stat.h>
 
 #include "common.cuh"
 #include "host/problem.h"
@@ -153,9 +156,15 @@ int dlp_problem_generate_cached(int num_nodes, int avg_degree, int num_batches, 
     return DLP_OK;
   }
   delete p;
-  // absent, stale or damaged: generate, then (re)write the file
+  // absent, stale or damaged: generate, then (re)write the file (the cache
+  // directory itself is created when missing; its parent must exist)
   const int st = dlp_problem_generate(num_nodes, avg_degree, num_batches, seed, gt_fraction, deleted_fraction, out);
   if (st != DLP_OK) return st;
+  if (mkdir(cache_dir, 0755) != 0 && errno != EEXIST) {
+    dlp_problem_free(*out);
+    *out = nullptr;
+    return dlp::fail(DLP_ERR_INVALID_ARGUMENT, std::string("cannot create ") + cache_dir + ": " + std::strerror(errno));
+  }
   if (!dlp::save_problem((*out)->p, key, path, &err)) {
     dlp_problem_free(*out);
     *out = nullptr;

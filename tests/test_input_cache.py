@@ -111,3 +111,11 @@ def test_c_abi_save_and_load(native, tmp_path):
     same(loaded, p2)
     with pytest.raises(dlp.DlpError):
         dlp.Problem.load(tmp_path / "missing.bin")
+    # the C entry point creates a missing cache directory (one level)
+    h = ctypes.c_void_p()
+    hit = ctypes.c_int(1)
+    d = str(tmp_path / "fresh").encode()
+    N.check(L.dlp_problem_generate_cached(2000, 3, 4, 11, ctypes.c_float(0.01), ctypes.c_float(0.09), d,
+                                          ctypes.byref(h), ctypes.byref(hit)))
+    L.dlp_problem_free(h)
+    assert hit.value == 0 and cache_files(tmp_path / "fresh") == [name]
