@@ -320,7 +320,7 @@ def irlp_block(p, batch_ms: list, threads: int, budget_s: float, device: int) ->
                      "incremental_ms": batch_ms[b]})
     gpu_ms = sum(r["gpu_ms"] for r in rows)
     inc_ms = sum(batch_ms)
-    return {"snapshot": "the driver's IrLP input after each batch (src/main.cu:127-176)",
+    return {"snapshot": "the IrLP input src/main.cu:127-176 builds, after each batch",
             "gpu_ms_all_batches": gpu_ms, "cpu_ms_all_batches": sum(r["cpu_ms"] for r in rows),
             "incremental_ms_all_batches": inc_ms,
             "gpu_irlp_over_incremental": gpu_ms / inc_ms if inc_ms > 0 else None,

@@ -55,9 +55,9 @@ def test_snapshot_is_the_drivers(native):
 
 def test_snapshot_against_oracle_rebuild(native, oracle):
     """The oracle's active graph (src/dynLP.cu:111-166, updateHostCSR) after the
-    same batch differs from the driver's IrLP snapshot only through vertices
+    same batch differs from main.cu's IrLP snapshot only through vertices
     inserted and deleted in one batch: updateHostCSR marks deletions before
-    insertions (such a vertex stays active), the driver's snapshot loop marks
+    insertions (such a vertex stays active), main.cu's snapshot loop marks
     them after (it is deleted). With those vertices' rows and entries taken
     out of both, the graphs are equal."""
     p = dlp.Problem(*CFG, cache_dir="")
