@@ -76,3 +76,12 @@ def test_mode_delta_per_step():
     assert d["team"] == {"passes": 5.0, "ms": "in one_block"}
     assert d["sub_grid"]["us_per_pass"] is None
     assert abs(d["full_grid"]["us_per_pass"] - 10000.0) < 1e-6
+
+
+def test_percentile_matches_numpy_linear():
+    rng = np.random.default_rng(2)
+    for n in (1, 2, 7, 100, 1001):
+        xs = rng.exponential(size=n).tolist()
+        for q in (0.0, 0.5, 0.9, 0.99, 1.0):
+            assert abs(bench.percentile(xs, q) - float(np.percentile(xs, 100 * q))) < 1e-12
+    assert bench.percentile([], 0.5) is None
